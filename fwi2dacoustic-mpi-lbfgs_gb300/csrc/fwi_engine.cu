@@ -1,0 +1,662 @@
+// fwi_engine.cu -- host side of the C ABI declared in include/fwi_gb300.h.
+//
+// Owns the device state of one batch of shots and drives the per-step
+// kernels of fwi_kernels.cuh.  Replaces, for the hot path, the per-rank plan
+// setup fwi_init (fwi_2d.c:139-396) and the missing per-shot driver
+// grad4_1shot (header.h:283): all shots of an iteration live on one GPU and
+// every time step of every shot is one launch (grid.z = shot).
+#include "fwi_gb300.h"
+#include "fwi_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace fwi;
+
+namespace {
+
+constexpr int kVersion = 1;
+
+inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
+
+// CPML damping profile on 2*npml+1 half-cell nodes, cpml_coe (fwi_2d.c:110-137)
+// with pml_base.dim = 2.  The reference mixes float locals with double libm
+// calls (log, exp) and double constants; the same promotions are kept here so
+// that the profile is bit-identical to the reference's.
+void cpml_profile(float* a0, float* b0, int npml, float d, float dt, float maxF, float maxV, float coefR)
+{
+    const float half = d * 0.5;
+    const int npower = 2;
+    const float width = npml * d;
+    const float pif0 = 3.141592654 * maxF;          // PI as fwi_sys.h:1 defines it
+    const float slope = pif0 / width;
+    const float d0 = -(npower + 1) * maxV * std::log((double)coefR) / (2.0 * width);
+    for (int i = 0; i < 2 * npml + 1; ++i) {
+        float damp = (1.0 - i * half / width);
+        damp *= damp;
+        damp *= d0;
+        const float alpha = slope * (i * half);
+        b0[i] = (float)std::exp((double)(-(damp + alpha) * dt));
+        a0[i] = (float)(damp / (damp + alpha) * (b0[i] - 1.0));
+    }
+}
+
+// FD coefficients as fwi_init sets them (fwi_2d.c:304-314): the optimized
+// 4th-order staggered pair (1.129042, -0.04301412) scaled by 1/h.
+void fd_coefficients(float dx, float dz, float out[8])
+{
+    const float ix = 1.0 / dx, iz = 1.0 / dz;
+    out[0] = 0.1129042e1 * ix;  out[1] = -0.4301412e-1 * ix;  out[2] = ix;
+    out[3] = 0.1129042e1 * iz;  out[4] = -0.4301412e-1 * iz;  out[5] = iz;
+    out[6] = iz / 840.0;        out[7] = iz / 24.0;
+}
+
+// Cell of a position in metres, fwi_2d.c:363-364.
+inline void cell_of(float x, float z, float dx, float dz, int* ix, int* iz)
+{
+    *ix = (int)std::round(x / dx);
+    *iz = (int)std::round(z / dz - 0.5);
+}
+
+}  // namespace
+
+struct fwi_ctx {
+    fwi_config cfg{};
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[6]{};
+    Geo g{};
+    Coef c{};
+    PsiLayout pl{};
+    int rows_alloc = 0;
+    long long origin = 0;          // floats from a shot block's start to (row 0, col 0)
+    float* K = nullptr;            // one shot block
+    float* vel = nullptr;          // [nz][nx]
+    float* pmlc = nullptr;         // 8 * (2*npml+1)
+    // per-shot state
+    int nshots = 0;
+    int nt_run = 0;
+    float* F = nullptr;            // 2 x nshots x fstride (forward field / rebuild)
+    float* A = nullptr;            // 2 x nshots x fstride (adjoint)
+    float* Gacc = nullptr;         // nshots x fstride
+    float* psiF = nullptr;         // 2 x nshots x pl.stride
+    float* psiA = nullptr;
+    float* ring = nullptr;
+    float* syn = nullptr;
+    float* res = nullptr;
+    float* obs = nullptr;
+    float* wav = nullptr;
+    double* grad = nullptr;
+    float* gradf = nullptr;
+    double* partial = nullptr;
+    double* mis = nullptr;
+    ShotDev* shots_d = nullptr;
+    RecDev* recs_d = nullptr;
+    int* rtile_d = nullptr;
+    std::vector<int> nt_slot;      // nt of each slot, descending
+    long long nsamples = 0;
+    int npartial = 0;
+    bool have_model = false, have_obs = false, have_fwd = false;
+    size_t bytes_model = 0, bytes_shots = 0;
+    std::string err;
+    fwi_stats stats{};
+};
+
+namespace {
+
+int fail(fwi_ctx* x, int code, const std::string& msg)
+{
+    if (x) x->err = msg;
+    return code;
+}
+
+int cuda_fail(fwi_ctx* x, cudaError_t e, const char* what)
+{
+    return fail(x, FWI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                       \
+    do {                                                               \
+        cudaError_t e_ = (call);                                       \
+        if (e_ != cudaSuccess) return cuda_fail(x, e_, #call);         \
+    } while (0)
+
+template <class T>
+int dalloc(fwi_ctx* x, T** p, size_t n, size_t* acc)
+{
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(x, FWI_ERR_NOMEM, std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes failed");
+    }
+    *acc += n * sizeof(T);
+    return FWI_OK;
+}
+
+void free_shots(fwi_ctx* x)
+{
+    void* ps[] = {x->F, x->A, x->Gacc, x->psiF, x->psiA, x->ring, x->syn, x->res, x->obs, x->wav,
+                  x->shots_d, x->recs_d, x->rtile_d, x->partial, x->mis};
+    for (void* p : ps) if (p) cudaFree(p);
+    x->F = x->A = x->Gacc = x->psiF = x->psiA = x->ring = x->syn = x->res = x->obs = x->wav = nullptr;
+    x->shots_d = nullptr; x->recs_d = nullptr; x->rtile_d = nullptr; x->partial = nullptr; x->mis = nullptr;
+    x->nshots = 0; x->nt_run = 0; x->nsamples = 0; x->bytes_shots = 0;
+    x->nt_slot.clear();
+    x->have_obs = x->have_fwd = false;
+}
+
+StepParams base_params(const fwi_ctx* x)
+{
+    StepParams P{};
+    P.g = x->g;
+    P.c = x->c;
+    P.K = x->K + x->origin;
+    P.pmlc = x->pmlc;
+    P.pl = x->pl;
+    P.shots = x->shots_d;
+    P.recs = x->recs_d;
+    P.rtile = x->rtile_d;
+    P.wav = x->wav;
+    P.syn = x->syn;
+    P.res = x->res;
+    P.ring = x->ring;
+    P.strip_len = 2 * NSTRIP * (x->g.nx + x->g.nz);
+    P.jump = x->cfg.jump;
+    return P;
+}
+
+int active_slots(const fwi_ctx* x, int pred_ge)   // shots with nt >= pred_ge
+{
+    int n = 0;
+    while (n < x->nshots && x->nt_slot[n] >= pred_ge) ++n;
+    return n;
+}
+
+int run_forward(fwi_ctx* x)
+{
+    const long long half = (long long)x->nshots * x->g.fstride;
+    const long long phalf = (long long)x->nshots * x->pl.stride;
+    CK(cudaMemsetAsync(x->F, 0, sizeof(float) * 2 * half, x->st));
+    CK(cudaMemsetAsync(x->psiF, 0, sizeof(float) * 2 * phalf, x->st));
+    StepParams P = base_params(x);
+    const dim3 block(BX, BY);
+    CK(cudaEventRecord(x->ev[0], x->st));
+    long long launches = 0;
+    for (int it = 0; it < x->nt_run; ++it) {
+        const int nact = active_slots(x, it + 1);
+        P.step = it;
+        P.pcur = x->F + (long long)(it & 1) * half + x->origin;
+        P.pold = x->F + (long long)((it + 1) & 1) * half + x->origin;
+        P.psr = x->psiF + (long long)(it & 1) * phalf;
+        P.psw = x->psiF + (long long)((it + 1) & 1) * phalf;
+        k_forward<<<dim3(x->g.ntx, x->g.ntz, nact), block, 0, x->st>>>(P);
+        ++launches;
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(x->ev[1], x->st));
+    x->stats.launches = launches;
+    return FWI_OK;
+}
+
+int run_misfit(fwi_ctx* x)
+{
+    CK(cudaEventRecord(x->ev[4], x->st));
+    k_misfit<<<x->npartial, 256, 0, x->st>>>(x->syn, x->obs, x->res, x->nsamples, x->partial);
+    k_misfit_final<<<1, 256, 0, x->st>>>(x->partial, x->npartial, x->mis);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(x->ev[5], x->st));
+    x->stats.launches += 2;
+    return FWI_OK;
+}
+
+int run_backward(fwi_ctx* x)
+{
+    const long long half = (long long)x->nshots * x->g.fstride;
+    const long long phalf = (long long)x->nshots * x->pl.stride;
+    CK(cudaMemsetAsync(x->A, 0, sizeof(float) * 2 * half, x->st));
+    CK(cudaMemsetAsync(x->psiA, 0, sizeof(float) * 2 * phalf, x->st));
+    CK(cudaMemsetAsync(x->Gacc, 0, sizeof(float) * half, x->st));
+    StepParams P = base_params(x);
+    P.gacc = x->Gacc + x->origin;
+    const dim3 block(BX, BY);
+    const size_t smem = sizeof(BwdSmem);
+    CK(cudaEventRecord(x->ev[2], x->st));
+    long long launches = 0;
+    for (int m = x->nt_run; m >= 1; --m) {
+        const int nact = active_slots(x, m);
+        P.step = m;
+        P.pcur = x->F + (long long)((m - 1) & 1) * half + x->origin;   // p^{m-1}
+        P.pold = x->F + (long long)(m & 1) * half + x->origin;         // p^m -> p^{m-2}
+        P.bcur = x->A + (long long)((m + 1) & 1) * half + x->origin;   // b^{m+1}
+        P.bold = x->A + (long long)(m & 1) * half + x->origin;         // b^{m+2} -> b^m
+        P.psr = x->psiA + (long long)(m & 1) * phalf;
+        P.psw = x->psiA + (long long)((m + 1) & 1) * phalf;
+        k_backward<<<dim3(x->g.ntx, x->g.ntz, nact), block, smem, x->st>>>(P);
+        ++launches;
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(x->ev[3], x->st));
+    // FP64 reduction over shots and the 2/v factor
+    k_reduce<<<dim3((x->g.nx + 255) / 256, x->g.nz), 256, 0, x->st>>>(x->Gacc + x->origin, x->vel, x->grad, x->g, x->nshots);
+    CK(cudaGetLastError());
+    x->stats.launches += launches + 1;
+    return FWI_OK;
+}
+
+float event_ms(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) { cudaGetLastError(); return 0.f; }
+    return ms;
+}
+
+int finish(fwi_ctx* x)
+{
+    CK(cudaStreamSynchronize(x->st));
+    return FWI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fwi_version(void) { return kVersion; }
+
+const char* fwi_status_string(int s)
+{
+    switch (s) {
+    case FWI_OK: return "ok";
+    case FWI_ERR_ARG: return "invalid argument";
+    case FWI_ERR_GEOMETRY: return "source or receiver outside the model";
+    case FWI_ERR_NOMEM: return "out of memory";
+    case FWI_ERR_CUDA: return "CUDA error";
+    case FWI_ERR_STATE: return "call out of order";
+    case FWI_ERR_CFL: return "model violates the CFL limit";
+    case FWI_ERR_NONFINITE: return "non-finite input";
+    case FWI_ERR_NODEVICE: return "no usable sm_103 device";
+    default: return "unknown status";
+    }
+}
+
+const char* fwi_last_error(const fwi_ctx* x) { return x ? x->err.c_str() : "null context"; }
+
+int fwi_cpml_profile(int npml, float d, float dt, float max_f, float max_v, float coef_r, float* a, float* b)
+{
+    if (npml < 1 || !(d > 0) || !(dt > 0) || !a || !b) return FWI_ERR_ARG;
+    cpml_profile(a, b, npml, d, dt, max_f, max_v, coef_r);
+    return FWI_OK;
+}
+
+int fwi_fd_coefficients(float dx, float dz, float* out8)
+{
+    if (!(dx > 0) || !(dz > 0) || !out8) return FWI_ERR_ARG;
+    fd_coefficients(dx, dz, out8);
+    return FWI_OK;
+}
+
+int fwi_cell_of(float x, float z, float dx, float dz, int* ix, int* iz)
+{
+    if (!(dx > 0) || !(dz > 0) || !ix || !iz) return FWI_ERR_ARG;
+    cell_of(x, z, dx, dz, ix, iz);
+    return FWI_OK;
+}
+
+int fwi_check_config(const fwi_config* cfg)
+{
+    if (!cfg) return FWI_ERR_ARG;
+    if (cfg->nx < 8 || cfg->nz < 8 || cfg->npml < 1 || cfg->npml > 256) return FWI_ERR_ARG;
+    if (!(cfg->dx > 0) || !(cfg->dz > 0) || !(cfg->dt > 0)) return FWI_ERR_ARG;
+    if (cfg->nt_max < 1 || cfg->jump < 1) return FWI_ERR_ARG;
+    if (!(cfg->pml_max_f > 0) || !(cfg->pml_max_v > 0) || !(cfg->pml_coef_r > 0 && cfg->pml_coef_r < 1)) return FWI_ERR_ARG;
+    if (cfg->free_surface != 0 && cfg->free_surface != 1) return FWI_ERR_ARG;
+    for (int i = 0; i < 7; ++i) if (cfg->reserved[i]) return FWI_ERR_ARG;
+    return FWI_OK;
+}
+
+fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
+{
+    int st = fwi_check_config(cfg);
+    if (st) { if (status) *status = st; return nullptr; }
+    fwi_ctx* x = new (std::nothrow) fwi_ctx();
+    if (!x) { if (status) *status = FWI_ERR_NOMEM; return nullptr; }
+    x->cfg = *cfg;
+    auto bail = [&](int code) -> fwi_ctx* {
+        if (status) *status = code;
+        fwi_destroy(x);
+        return nullptr;
+    };
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) {
+        cudaGetLastError();
+        return bail(FWI_ERR_NODEVICE);
+    }
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, cfg->device) != cudaSuccess || prop.major != 10 || prop.minor != 3) {
+        cudaGetLastError();
+        return bail(FWI_ERR_NODEVICE);
+    }
+    if (cudaSetDevice(cfg->device) != cudaSuccess) return bail(FWI_ERR_NODEVICE);
+    if (cudaStreamCreateWithFlags(&x->st, cudaStreamNonBlocking) != cudaSuccess) return bail(FWI_ERR_CUDA);
+    for (auto& e : x->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return bail(FWI_ERR_CUDA);
+
+    Geo& g = x->g;
+    g.nx = cfg->nx; g.nz = cfg->nz; g.npml = cfg->npml; g.fs = cfg->free_surface;
+    g.pnx = cfg->nx + 2 * cfg->npml;                         // fwi_2d.c:155
+    g.pnz = cfg->nz + (g.fs ? 1 : 2) * cfg->npml;            // fwi_2d.c:155,162
+    g.x0p = cfg->npml; g.z0p = g.fs ? 0 : cfg->npml;
+    g.ntx = (g.pnx + TX - 1) / TX;
+    g.ntz = (g.pnz + TZ - 1) / TZ;
+    g.ld = (int)round_up(MX + (long long)g.ntx * TX + HX, 32);
+    x->rows_alloc = MZ + g.ntz * TZ + MZ;
+    g.fstride = (long long)x->rows_alloc * g.ld;
+    x->origin = (long long)MZ * g.ld + MX;
+
+    float fd[8];
+    fd_coefficients(cfg->dx, cfg->dz, fd);
+    Coef& c = x->c;
+    c.c0x = fd[0]; c.c1x = fd[1]; c.ix = fd[2]; c.c0z = fd[3]; c.c1z = fd[4]; c.iz = fd[5];
+    c.iz840 = fd[6]; c.iz24 = fd[7];
+    c.iarea = 1.0 / (cfg->dx * cfg->dz);                    // fwi_2d.c:216
+
+    const int np = cfg->npml, n2 = 2 * np + 1;
+    PsiLayout& pl = x->pl;
+    long long off = 0;
+    pl.u0 = (int)off;  off += (long long)g.pnz * (np + 1);
+    pl.u1 = (int)off;  off += (long long)g.pnz * (np + 1);
+    pl.v0 = (int)off;  off += (long long)(np + 1) * g.pnx;
+    pl.v1 = (int)off;  off += (long long)(np + 1) * g.pnx;
+    pl.ux0 = (int)off; off += (long long)g.pnz * np;
+    pl.ux1 = (int)off; off += (long long)g.pnz * np;
+    pl.vz0 = (int)off; off += (long long)np * g.pnx;
+    pl.vz1 = (int)off; off += (long long)np * g.pnx;
+    pl.stride = round_up(off, 32);
+
+    // CPML profiles: a0/b0 from cpml_coe, a1/b1 mirrored (fwi_2d.c:272-283)
+    std::vector<float> h(8 * n2);
+    float *a0x = &h[0], *b0x = &h[n2], *a1x = &h[2 * n2], *b1x = &h[3 * n2];
+    float *a0z = &h[4 * n2], *b0z = &h[5 * n2], *a1z = &h[6 * n2], *b1z = &h[7 * n2];
+    cpml_profile(a0x, b0x, np, cfg->dx, cfg->dt, cfg->pml_max_f, cfg->pml_max_v, cfg->pml_coef_r);
+    cpml_profile(a0z, b0z, np, cfg->dz, cfg->dt, cfg->pml_max_f, cfg->pml_max_v, cfg->pml_coef_r);
+    for (int i = 0; i < n2; ++i) {
+        a1x[i] = a0x[2 * np - i]; b1x[i] = b0x[2 * np - i];
+        a1z[i] = a0z[2 * np - i]; b1z[i] = b0z[2 * np - i];
+    }
+    if (dalloc(x, &x->pmlc, h.size(), &x->bytes_model)) return bail(FWI_ERR_NOMEM);
+    if (dalloc(x, &x->K, (size_t)g.fstride, &x->bytes_model)) return bail(FWI_ERR_NOMEM);
+    if (dalloc(x, &x->vel, (size_t)g.nx * g.nz, &x->bytes_model)) return bail(FWI_ERR_NOMEM);
+    if (dalloc(x, &x->grad, (size_t)g.nx * g.nz, &x->bytes_model)) return bail(FWI_ERR_NOMEM);
+    if (dalloc(x, &x->gradf, (size_t)g.nx * g.nz, &x->bytes_model)) return bail(FWI_ERR_NOMEM);
+    if (cudaMemcpy(x->pmlc, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return bail(FWI_ERR_CUDA);
+    if (cudaMemset(x->K, 0, sizeof(float) * g.fstride) != cudaSuccess) return bail(FWI_ERR_CUDA);
+    if (cudaFuncSetAttribute(k_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BwdSmem)) != cudaSuccess)
+        return bail(FWI_ERR_CUDA);
+    if (status) *status = FWI_OK;
+    return x;
+}
+
+void fwi_destroy(fwi_ctx* x)
+{
+    if (!x) return;
+    free_shots(x);
+    void* ps[] = {x->K, x->vel, x->pmlc, x->grad, x->gradf};
+    for (void* p : ps) if (p) cudaFree(p);
+    for (auto& e : x->ev) if (e) cudaEventDestroy(e);
+    if (x->st) cudaStreamDestroy(x->st);
+    delete x;
+}
+
+int fwi_set_model(fwi_ctx* x, const float* vel)
+{
+    if (!x || !vel) return fail(x, FWI_ERR_ARG, "null argument");
+    const Geo& g = x->g;
+    const size_t n = (size_t)g.nx * g.nz;
+    float vmax = 0.f;
+    for (size_t i = 0; i < n; ++i) {
+        const float v = vel[i];
+        if (!std::isfinite(v)) return fail(x, FWI_ERR_NONFINITE, "non-finite velocity at index " + std::to_string(i));
+        if (!(v > 0.f)) return fail(x, FWI_ERR_ARG, "non-positive velocity at index " + std::to_string(i));
+        vmax = std::max(vmax, v);
+    }
+    // leapfrog stability of the 4th-order staggered pair: v dt (|c0|+|c1|) sqrt(1/dx^2+1/dz^2) <= 1
+    const double cfl = (double)vmax * x->cfg.dt * (1.129042 + 0.04301412) *
+                       std::sqrt(1.0 / ((double)x->cfg.dx * x->cfg.dx) + 1.0 / ((double)x->cfg.dz * x->cfg.dz));
+    if (cfl > 1.0) return fail(x, FWI_ERR_CFL, "CFL number " + std::to_string(cfl) + " > 1");
+    CK(cudaSetDevice(x->cfg.device));
+    CK(cudaMemcpyAsync(x->vel, vel, n * sizeof(float), cudaMemcpyHostToDevice, x->st));
+    k_build_K<<<dim3((g.pnx + 255) / 256, g.pnz), 256, 0, x->st>>>(x->vel, x->K + x->origin, g, x->cfg.dt);
+    CK(cudaGetLastError());
+    int s = finish(x);
+    if (s) return s;
+    x->have_model = true;
+    x->have_fwd = false;
+    return FWI_OK;
+}
+
+int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
+{
+    if (!x || nshots < 1 || !shots) return fail(x, FWI_ERR_ARG, "need at least one shot");
+    CK(cudaSetDevice(x->cfg.device));
+    const Geo& g = x->g;
+    const int jump = x->cfg.jump;
+    // validate and convert geometry (fwi_2d.c:357-371)
+    std::vector<ShotDev> sd(nshots);
+    std::vector<std::vector<RecDev>> recs(nshots);
+    std::vector<std::vector<int>> rtiles(nshots);
+    long long syn_off = 0, wav_tot = 0;
+    std::vector<long long> wav_off(nshots);
+    for (int s = 0; s < nshots; ++s) {
+        const fwi_shot& sh = shots[s];
+        if (sh.nt < 1 || sh.nt > x->cfg.nt_max || (sh.nt - 1) % jump != 0)
+            return fail(x, FWI_ERR_ARG, "shot " + std::to_string(s) + ": nt must be in [1, nt_max] with (nt-1) % jump == 0");
+        if (sh.nr < 0 || (sh.nr > 0 && !sh.rec_xz) || !sh.wavelet)
+            return fail(x, FWI_ERR_ARG, "shot " + std::to_string(s) + ": missing receivers or wavelet");
+        int ix, iz;
+        cell_of(sh.src_x, sh.src_z, x->cfg.dx, x->cfg.dz, &ix, &iz);
+        if (ix < 0 || ix >= g.nx || iz < 0 || iz >= g.nz)
+            return fail(x, FWI_ERR_GEOMETRY, "shot " + std::to_string(s) + ": source outside the model");
+        for (int i = 0; i < sh.nt; ++i)
+            if (!std::isfinite(sh.wavelet[i])) return fail(x, FWI_ERR_NONFINITE, "non-finite wavelet sample");
+        ShotDev& d = sd[s];
+        d.nt = sh.nt; d.nt0 = (sh.nt - 1) / jump + 1; d.nr = sh.nr;
+        d.src_r = iz + g.z0p; d.src_c = ix + g.x0p;
+        d.syn_off = syn_off;
+        wav_off[s] = wav_tot;
+        d.wav_off = (int)wav_tot;
+        wav_tot += sh.nt;
+        std::vector<std::pair<int, RecDev>> tmp(sh.nr);
+        for (int r = 0; r < sh.nr; ++r) {
+            int rx, rz;
+            cell_of(sh.rec_xz[2 * r], sh.rec_xz[2 * r + 1], x->cfg.dx, x->cfg.dz, &rx, &rz);
+            if (rx < 0 || rx >= g.nx || rz < 0 || rz >= g.nz)
+                return fail(x, FWI_ERR_GEOMETRY, "shot " + std::to_string(s) + ": receiver " + std::to_string(r) + " outside the model");
+            const int row = rz + g.z0p, col = rx + g.x0p;
+            const int tile = (row / TZ) * g.ntx + col / TX;
+            RecDev rd{};
+            rd.cell = (row % TZ) * TX + (col % TX);
+            rd.syn_base = syn_off + (long long)r * d.nt0;
+            tmp[r] = {tile, rd};
+        }
+        std::stable_sort(tmp.begin(), tmp.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+        const int ntiles = g.ntx * g.ntz;
+        rtiles[s].assign(ntiles + 1, 0);
+        for (auto& t : tmp) rtiles[s][t.first + 1]++;
+        for (int t = 0; t < ntiles; ++t) rtiles[s][t + 1] += rtiles[s][t];
+        for (auto& t : tmp) recs[s].push_back(t.second);
+        syn_off += (long long)sh.nr * d.nt0;
+    }
+    // slots: shots sorted by nt, longest first, so the active shots of a step form a prefix
+    std::vector<int> order(nshots);
+    for (int s = 0; s < nshots; ++s) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sd[a].nt > sd[b].nt; });
+
+    free_shots(x);
+    const int ntiles = g.ntx * g.ntz;
+    const long long strip_len = 2LL * NSTRIP * (g.nx + g.nz);
+    std::vector<ShotDev> slot(nshots);
+    std::vector<RecDev> rec_all;
+    std::vector<int> rt_all;
+    std::vector<float> wav_all(wav_tot);
+    long long ring_off = 0;
+    x->nt_slot.resize(nshots);
+    for (int k = 0; k < nshots; ++k) {
+        const int s = order[k];
+        ShotDev d = sd[s];
+        d.ring_off = ring_off;
+        ring_off += (long long)d.nt * strip_len;
+        d.rtile_off = (int)rt_all.size();
+        const int rbase = (int)rec_all.size();
+        for (int t = 0; t <= ntiles; ++t) rt_all.push_back(rtiles[s][t] + rbase);
+        rec_all.insert(rec_all.end(), recs[s].begin(), recs[s].end());
+        std::memcpy(&wav_all[wav_off[s]], shots[s].wavelet, sizeof(float) * shots[s].nt);
+        slot[k] = d;
+        x->nt_slot[k] = d.nt;
+    }
+    x->nshots = nshots;
+    x->nt_run = x->nt_slot[0];
+    x->nsamples = syn_off;
+    x->npartial = (int)std::min<long long>(1024, std::max<long long>(1, (syn_off + 255) / 256));
+    size_t& b = x->bytes_shots;
+    const size_t half = (size_t)nshots * g.fstride, phalf = (size_t)nshots * x->pl.stride;
+    int e = 0;
+    e = e ? e : dalloc(x, &x->F, 2 * half, &b);
+    e = e ? e : dalloc(x, &x->A, 2 * half, &b);
+    e = e ? e : dalloc(x, &x->Gacc, half, &b);
+    e = e ? e : dalloc(x, &x->psiF, 2 * phalf, &b);
+    e = e ? e : dalloc(x, &x->psiA, 2 * phalf, &b);
+    e = e ? e : dalloc(x, &x->ring, (size_t)ring_off, &b);
+    e = e ? e : dalloc(x, &x->syn, (size_t)syn_off, &b);
+    e = e ? e : dalloc(x, &x->res, (size_t)syn_off, &b);
+    e = e ? e : dalloc(x, &x->obs, (size_t)syn_off, &b);
+    e = e ? e : dalloc(x, &x->wav, (size_t)wav_tot, &b);
+    e = e ? e : dalloc(x, &x->shots_d, (size_t)nshots, &b);
+    e = e ? e : dalloc(x, &x->recs_d, rec_all.size(), &b);
+    e = e ? e : dalloc(x, &x->rtile_d, rt_all.size(), &b);
+    e = e ? e : dalloc(x, &x->partial, (size_t)x->npartial, &b);
+    e = e ? e : dalloc(x, &x->mis, 2, &b);
+    if (e) { std::string m = x->err; free_shots(x); x->err = m; return e; }
+    CK(cudaMemcpyAsync(x->shots_d, slot.data(), sizeof(ShotDev) * nshots, cudaMemcpyHostToDevice, x->st));
+    if (!rec_all.empty())
+        CK(cudaMemcpyAsync(x->recs_d, rec_all.data(), sizeof(RecDev) * rec_all.size(), cudaMemcpyHostToDevice, x->st));
+    CK(cudaMemcpyAsync(x->rtile_d, rt_all.data(), sizeof(int) * rt_all.size(), cudaMemcpyHostToDevice, x->st));
+    CK(cudaMemcpyAsync(x->wav, wav_all.data(), sizeof(float) * wav_all.size(), cudaMemcpyHostToDevice, x->st));
+    CK(cudaMemsetAsync(x->syn, 0, sizeof(float) * std::max<long long>(1, syn_off), x->st));
+    return finish(x);
+}
+
+int fwi_set_observed(fwi_ctx* x, const float* obs)
+{
+    if (!x || !obs) return fail(x, FWI_ERR_ARG, "null argument");
+    if (!x->nshots) return fail(x, FWI_ERR_STATE, "fwi_set_shots first");
+    CK(cudaSetDevice(x->cfg.device));
+    CK(cudaMemcpyAsync(x->obs, obs, sizeof(float) * x->nsamples, cudaMemcpyHostToDevice, x->st));
+    int s = finish(x);
+    if (s) return s;
+    x->have_obs = true;
+    return FWI_OK;
+}
+
+static void record_stats(fwi_ctx* x, bool fwd, bool mis, bool bwd)
+{
+    long long cells = 0;
+    for (int nt : x->nt_slot) cells += (long long)nt;
+    const double cs = (double)cells * x->g.nx * x->g.nz;
+    x->stats.ms_forward = fwd ? event_ms(x->ev[0], x->ev[1]) : 0.0;
+    x->stats.ms_misfit = mis ? event_ms(x->ev[4], x->ev[5]) : 0.0;
+    x->stats.ms_backward = bwd ? event_ms(x->ev[2], x->ev[3]) : 0.0;
+    x->stats.cell_steps = cs * ((fwd ? 1 : 0) + (bwd ? 2 : 0));
+    x->stats.device_bytes = (long long)(x->bytes_model + x->bytes_shots);
+}
+
+int fwi_forward(fwi_ctx* x, float* syn_out)
+{
+    if (!x) return FWI_ERR_ARG;
+    if (!x->have_model || !x->nshots) return fail(x, FWI_ERR_STATE, "fwi_set_model and fwi_set_shots first");
+    CK(cudaSetDevice(x->cfg.device));
+    int s = run_forward(x);
+    if (s) return s;
+    if (syn_out) CK(cudaMemcpyAsync(syn_out, x->syn, sizeof(float) * x->nsamples, cudaMemcpyDeviceToHost, x->st));
+    s = finish(x);
+    if (s) return s;
+    record_stats(x, true, false, false);
+    x->have_fwd = true;
+    return FWI_OK;
+}
+
+int fwi_backward(fwi_ctx* x, const float* residual, double* grad_out)
+{
+    if (!x || !residual) return fail(x, FWI_ERR_ARG, "null argument");
+    if (!x->have_fwd) return fail(x, FWI_ERR_STATE, "fwi_forward on the current model first");
+    CK(cudaSetDevice(x->cfg.device));
+    CK(cudaMemcpyAsync(x->res, residual, sizeof(float) * x->nsamples, cudaMemcpyHostToDevice, x->st));
+    int s = run_backward(x);
+    if (s) return s;
+    if (grad_out)
+        CK(cudaMemcpyAsync(grad_out, x->grad, sizeof(double) * x->g.nx * x->g.nz, cudaMemcpyDeviceToHost, x->st));
+    s = finish(x);
+    x->have_fwd = false;   // the rebuild consumed the final forward fields
+    if (s) return s;
+    record_stats(x, false, false, true);
+    return FWI_OK;
+}
+
+static int gradient_impl(fwi_ctx* x, double* misfit)
+{
+    if (!x) return FWI_ERR_ARG;
+    if (!x->have_model || !x->nshots || !x->have_obs)
+        return fail(x, FWI_ERR_STATE, "fwi_set_model, fwi_set_shots and fwi_set_observed first");
+    CK(cudaSetDevice(x->cfg.device));
+    x->have_fwd = false;
+    int s = run_forward(x);
+    if (s) return s;
+    s = run_misfit(x);
+    if (s) return s;
+    s = run_backward(x);
+    if (s) return s;
+    if (misfit) CK(cudaMemcpyAsync(misfit, x->mis, 2 * sizeof(double), cudaMemcpyDeviceToHost, x->st));
+    return FWI_OK;
+}
+
+int fwi_gradient(fwi_ctx* x, double* misfit, double* grad_out)
+{
+    int s = gradient_impl(x, misfit);
+    if (s) return s;
+    if (grad_out)
+        CK(cudaMemcpyAsync(grad_out, x->grad, sizeof(double) * x->g.nx * x->g.nz, cudaMemcpyDeviceToHost, x->st));
+    s = finish(x);
+    if (s) return s;
+    record_stats(x, true, true, true);
+    return FWI_OK;
+}
+
+int fwi_gradient_f32(fwi_ctx* x, double* misfit, float* grad_out)
+{
+    int s = gradient_impl(x, misfit);
+    if (s) return s;
+    const long long n = (long long)x->g.nx * x->g.nz;
+    if (grad_out) {
+        k_to_float<<<256, 256, 0, x->st>>>(x->grad, x->gradf, n);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(grad_out, x->gradf, sizeof(float) * n, cudaMemcpyDeviceToHost, x->st));
+    }
+    s = finish(x);
+    if (s) return s;
+    record_stats(x, true, true, true);
+    return FWI_OK;
+}
+
+const double* fwi_grad_device(const fwi_ctx* x) { return x ? x->grad : nullptr; }
+
+int fwi_get_stats(const fwi_ctx* x, fwi_stats* out)
+{
+    if (!x || !out) return FWI_ERR_ARG;
+    *out = x->stats;
+    return FWI_OK;
+}
+
+}  // extern "C"

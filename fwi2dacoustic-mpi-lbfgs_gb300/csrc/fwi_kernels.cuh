@@ -1,0 +1,804 @@
+// fwi_kernels.cuh -- sm_103a kernels of the FWI gradient hot path.
+//
+// One launch advances every active shot of the batch by one time step
+// (grid.z = shot slot).  A thread block owns a TZ x TX tile of the padded
+// grid of one shot; the pressure tile and its halo are staged in shared
+// memory once, the x-direction intermediate (u, the staggered d/dx) goes
+// through shared memory, and the z-direction chain (v = d/dz, vz) stays in
+// registers along each thread's column segment.  u, v, ux and vz of the
+// reference (fwi_2d.c:761-864) never reach HBM; the leapfrog update
+// (time_integral, fwi_2d.c:866-880), source injection, receiver sampling and
+// the boundary-strip save (write_bdr, fwi_2d.c:882-917) are fused into the
+// epilogue.  Forward HBM traffic per cell-step: read p^it, read+write
+// p^{it-1} -> p^{it+1} in place, read K (shared by all shots, L2-resident).
+//
+// Tiles that touch a grid edge (one-sided/edge stencils) or a CPML layer
+// (psi recursions) take the GENERAL path with per-position formulas; all
+// other tiles take the branch-free interior path.  The choice is uniform per
+// block.
+//
+// The backward kernel fuses, per cell and step m = nt .. 1,
+//   * the exact adjoint b^m = 2 b^{m+1} - b^{m+2} + K (L^T b^{m+1} + r^m) on
+//     the padded grid (L^T is the transpose of the CPML operator, including
+//     the adjoint of its psi recursions),
+//   * the source-field rebuild p^{m-2} = 2 p^{m-1} - p^m + K L p^{m-1} + s^{m-1}
+//     on the physical interior (a_lap_opt_2d, fwi_2d.c:722-759), with the
+//     three outer rows/columns restored from the strip ring (read_bdr,
+//     fwi_2d.c:919-960),
+//   * the imaging condition g += b^m (L p^{m-1} + f^{m-1}).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fwi {
+
+constexpr int TX = 64;             // tile width  (cells)
+constexpr int TZ = 32;             // tile height (cells)
+constexpr int BX = 32;             // threads in x
+constexpr int BY = 8;              // threads in z
+constexpr int NTH = BX * BY;
+constexpr int R = TZ / BY;         // rows per thread
+constexpr int CX = TX / BX;        // columns per thread
+constexpr int HX = 4;              // x halo staged (>= 3, multiple of 4 for float4)
+constexpr int HZ = 3;              // z halo staged
+constexpr int SPW = TX + 2 * HX;   // staged tile width  (72)
+constexpr int SPH = TZ + 2 * HZ;   // staged tile height (38)
+constexpr int UW = TX + 3;         // u positions x0-1 .. x0+TX+1
+constexpr int UWP = TX + 4;        // u row pitch
+constexpr int RXW = TX + 6;        // adjoint x-stage positions x0-3 .. x0+TX+2
+constexpr int RXP = TX + 8;
+constexpr int MX = 8;              // zero margin columns left of the grid in HBM arrays
+constexpr int MZ = 4;              // zero margin rows above the grid
+constexpr int NSTRIP = 3;          // 2*mm-1 saved rows/columns per side (fwi_sys.h:7, mm = 2)
+
+struct Geo {
+    int nx, nz;        // physical grid
+    int pnx, pnz;      // padded grid (fwi_2d.c:154-165)
+    int npml, fs;
+    int x0p, z0p;      // physical origin in padded coordinates
+    int ld;            // row pitch of every field array (floats)
+    int ntx, ntz;      // tiles per shot
+    long long fstride; // floats between consecutive shots in a field array
+};
+
+struct Coef {
+    float c0x, c1x, ix, c0z, c1z, iz, iz840, iz24;   // fwi_2d.c:304-314
+    float iarea;                                     // fwi_2d.c:216
+};
+
+// psi arrays of one shot, in the order u0,u1,v0,v1,ux0,ux1,vz0,vz1
+// (pml_profile, header.h:97; shapes fwi_2d.c:288-296).
+struct PsiLayout {
+    long long stride;  // floats per shot
+    int u0, u1, v0, v1, ux0, ux1, vz0, vz1;
+};
+
+struct ShotDev {
+    int nt, nt0, nr;
+    int src_r, src_c;        // source cell, padded coordinates
+    int wav_off;             // offset of the wavelet in the wavelet pool
+    int rtile_off;           // offset of this shot's per-tile receiver CSR
+    int pad;
+    long long syn_off;       // offset of the shot's traces in syn/res/obs
+    long long ring_off;      // offset of the shot's strip ring
+};
+
+struct RecDev {
+    int cell;                // (row % TZ) * TX + (col % TX) inside its tile
+    int pad;
+    long long syn_base;      // syn_off + r * nt0
+};
+
+struct StepParams {
+    Geo g;
+    Coef c;
+    const float* K;          // padded K = v^2 dt^2 (one copy for all shots)
+    const float* pcur;       // p^it (forward) / p^{m-1} (backward)
+    float* pold;             // p^{it-1} -> p^{it+1} / p^m -> p^{m-2}, in place
+    const float* bcur;       // b^{m+1}
+    float* bold;             // b^{m+2} -> b^m, in place
+    float* gacc;             // imaging accumulator, field layout, per shot
+    const float* psr;        // psi (or adjoint psi) read at this step
+    float* psw;              // psi written at this step
+    const float* pmlc;       // a0x b0x a1x b1x a0z b0z a1z b1z, 2*npml+1 each
+    PsiLayout pl;
+    const ShotDev* shots;
+    const RecDev* recs;
+    const int* rtile;
+    const float* wav;
+    float* syn;              // forward: sampled traces
+    const float* res;        // backward: adjoint sources
+    float* ring;             // boundary strips
+    int strip_len;
+    int step;                // forward: it; backward: m
+    int jump;
+};
+
+__device__ __forceinline__ bool tile_general(const Geo& g, int x0, int z0)
+{
+    const int np = g.npml;
+    if (x0 < 8 || x0 + TX + 8 > g.pnx) return true;               // x edges
+    if (x0 - 4 <= np || x0 + TX + 4 >= g.pnx - np) return true;   // x CPML
+    if (z0 < 8 || z0 + TZ + 8 > g.pnz) return true;               // z edges
+    if (z0 + TZ + 4 >= g.pnz - np) return true;                   // bottom CPML
+    if (!g.fs && z0 - 4 <= np) return true;                       // top CPML
+    return false;
+}
+
+// u = staggered d/dx of p at u-position j (fwi_2d.c:775-784); pr[c] = p[row][c].
+__device__ __forceinline__ float u_edge(const float* pr, int j, int pnx, const Coef& c)
+{
+    if (j >= 2 && j <= pnx - 2) return c.c0x * (pr[j] - pr[j - 1]) + c.c1x * (pr[j + 1] - pr[j - 2]);
+    if (j == 1) return c.ix * (pr[1] - pr[0]);
+    if (j == pnx - 1) return c.ix * (pr[pnx - 1] - pr[pnx - 2]);
+    return 0.f;   // u[0], u[pnx] are never assigned by the reference
+}
+
+// Stages the (TZ+2HZ) x (TX+2HX) tile of field f whose interior starts at
+// (z0, x0) into shared memory with 16-byte loads.
+__device__ __forceinline__ void stage_tile(const float* __restrict__ f, const Geo& g, int x0, int z0, float* sp)
+{
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    constexpr int Q = SPW / 4;
+    for (int i = tid; i < SPH * Q; i += NTH) {
+        const int r = i / Q, q = i - r * Q;
+        const float4 v = __ldg(reinterpret_cast<const float4*>(f + (long long)(z0 - HZ + r) * g.ld + (x0 - HX) + 4 * q));
+        *reinterpret_cast<float4*>(sp + r * SPW + 4 * q) = v;
+    }
+}
+
+__device__ __forceinline__ void save_strip(const StepParams& P, const ShotDev& sd, int row, int c, float val, int t)
+{
+    const Geo& g = P.g;
+    const int iz = row - g.z0p, ix = c - g.x0p;
+    if (iz < 0 || iz >= g.nz || ix < 0 || ix >= g.nx) return;
+    float* ring = P.ring + sd.ring_off + (long long)t * P.strip_len;
+    if (iz < NSTRIP) ring[iz * g.nx + ix] = val;
+    if (iz >= g.nz - NSTRIP) ring[(NSTRIP + g.nz - 1 - iz) * g.nx + ix] = val;
+    float* lr = ring + 2 * NSTRIP * g.nx;
+    if (ix < NSTRIP) lr[ix * g.nz + iz] = val;
+    if (ix >= g.nx - NSTRIP) lr[(NSTRIP + g.nx - 1 - ix) * g.nz + iz] = val;
+}
+
+__device__ __forceinline__ float load_strip(const StepParams& P, const ShotDev& sd, int iz, int ix, int t)
+{
+    const Geo& g = P.g;
+    const float* ring = P.ring + sd.ring_off + (long long)t * P.strip_len;
+    if (iz < NSTRIP) return ring[iz * g.nx + ix];
+    if (iz >= g.nz - NSTRIP) return ring[(NSTRIP + g.nz - 1 - iz) * g.nx + ix];
+    const float* lr = ring + 2 * NSTRIP * g.nx;
+    if (ix < NSTRIP) return lr[ix * g.nz + iz];
+    return lr[(NSTRIP + g.nx - 1 - ix) * g.nz + iz];
+}
+
+// ---------------------------------------------------------------------------
+// Forward step
+// ---------------------------------------------------------------------------
+template <bool GEN>
+__device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd, int s, int x0, int z0,
+                                         float* sp, float* su, float* vals)
+{
+    const Geo& g = P.g;
+    const Coef& cf = P.c;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int np = g.npml, n2 = 2 * np + 1;
+    const long long so = (long long)s * g.fstride;
+    const float* __restrict__ psr = P.psr + (long long)s * P.pl.stride;
+    float* __restrict__ psw = P.psw + (long long)s * P.pl.stride;
+    const float* a0x = P.pmlc;          const float* b0x = a0x + n2;
+    const float* a1x = a0x + 2 * n2;    const float* b1x = a0x + 3 * n2;
+    const float* a0z = a0x + 4 * n2;    const float* b0z = a0x + 5 * n2;
+    const float* a1z = a0x + 6 * n2;    const float* b1z = a0x + 7 * n2;
+
+    // u at positions j in [x0-1, x0+TX+1], rows [z0, z0+TZ)
+    #pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int rl = ty + BY * k, row = z0 + rl;
+        const float* pr = sp + (rl + HZ) * SPW + HX - x0;
+        #pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            const int jj = tx + BX * h;
+            if (jj >= UW) break;
+            const int j = x0 - 1 + jj;
+            float u;
+            if (!GEN) {
+                u = cf.c0x * (pr[j] - pr[j - 1]) + cf.c1x * (pr[j + 1] - pr[j - 2]);
+            } else {
+                u = u_edge(pr, j, g.pnx, cf);
+                if (row < g.pnz) {
+                    const bool own = jj >= 1 && jj <= TX;
+                    if (j >= 0 && j <= np) {                               // fwi_2d.c:790-791
+                        const int idx = P.pl.u0 + row * (np + 1) + j;
+                        const float ps = b0x[2 * j] * psr[idx] + a0x[2 * j] * u;
+                        if (own) psw[idx] = ps;
+                        u += ps;
+                    } else if (j >= g.pnx - np && j <= g.pnx) {           // fwi_2d.c:793-794
+                        const int kk = j - (g.pnx - np);
+                        const int idx = P.pl.u1 + row * (np + 1) + kk;
+                        const float ps = b1x[2 * kk] * psr[idx] + a1x[2 * kk] * u;
+                        if (own) psw[idx] = ps;
+                        u += ps;
+                    }
+                }
+            }
+            su[rl * UWP + jj] = u;
+        }
+    }
+    __syncthreads();
+
+    const int r0l = R * ty, r0 = z0 + r0l;
+    const float* __restrict__ K = P.K;
+    float* __restrict__ pold = P.pold + so;
+    const float amp = P.wav[sd.wav_off + P.step] * cf.iarea;
+    #pragma unroll
+    for (int h = 0; h < CX; ++h) {
+        const int cl = tx + BX * h, c = x0 + cl;
+        float pc[R + 6];
+        #pragma unroll
+        for (int k = 0; k < R + 6; ++k) pc[k] = sp[(r0l + k) * SPW + HX + cl];   // rows r0-3+k
+        float vv[R + 3];                                                            // v rows r0-1+k
+        #pragma unroll
+        for (int k = 0; k < R + 3; ++k) {
+            const int kv = r0 - 1 + k;
+            float v;
+            if (!GEN) {
+                v = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
+            } else {
+                if (kv >= 2 && kv <= g.pnz - 2) {
+                    v = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
+                } else if (kv == 0) {                                     // fwi_2d.c:805 (here r0 == 0)
+                    v = g.fs ? (3675.f * pc[3] - 1225.f * pc[4] + 441.f * pc[5] - 75.f * pc[6]) * cf.iz840 : 0.f;
+                } else if (kv == 1) {                                     // fwi_2d.c:807
+                    v = g.fs ? (-1085.f * pc[3] + 1015.f * pc[4] - 63.f * pc[5] + 5.f * pc[6]) * cf.iz840
+                             : cf.iz * (pc[4] - pc[3]);
+                } else if (kv == g.pnz - 1) {                             // fwi_2d.c:809
+                    v = (pc[k + 2] - pc[k + 1]) * cf.iz;
+                } else {
+                    v = 0.f;
+                }
+                if (c < g.pnx && kv >= 0 && kv <= g.pnz) {
+                    const bool own = k >= 1 && k <= R && kv < g.pnz;
+                    if (kv >= g.pnz - np) {                               // fwi_2d.c:816-817
+                        const int kk = kv - (g.pnz - np);
+                        const int idx = P.pl.v1 + kk * g.pnx + c;
+                        const float ps = b1z[2 * kk] * psr[idx] + a1z[2 * kk] * v;
+                        if (own) psw[idx] = ps;
+                        v += ps;
+                    } else if (!g.fs && kv <= np) {                       // top layer, all-sides CPML
+                        const int idx = P.pl.v0 + kv * g.pnx + c;
+                        const float ps = b0z[2 * kv] * psr[idx] + a0z[2 * kv] * v;
+                        if (own) psw[idx] = ps;
+                        v += ps;
+                    }
+                }
+            }
+            vv[k] = v;
+        }
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int row = r0 + i;
+            const float* ur = su + (r0l + i) * UWP + 1 - x0;                // ur[j] = u[row][j]
+            float vz, ux;
+            if (!GEN) {
+                vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
+                ux = cf.c0x * (ur[c + 1] - ur[c]) + cf.c1x * (ur[c + 2] - ur[c - 1]);
+            } else {
+                if (row >= 1 && row <= g.pnz - 2) {
+                    vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
+                } else if (row == 0) {                                    // fwi_2d.c:848 (i == 0 here)
+                    if (i == 0) {
+                        vz = g.fs ? (-22.f * vv[1] + 17.f * vv[2] + 9.f * vv[3] - 5.f * vv[4] + vv[5]) * cf.iz24
+                                  : (vv[2] - vv[1]) * cf.iz;
+                    } else {
+                        vz = 0.f;
+                    }
+                } else if (row == g.pnz - 1) {                            // fwi_2d.c:849
+                    vz = (vv[i + 2] - vv[i + 1]) * cf.iz;
+                } else {
+                    vz = 0.f;
+                }
+                if (c >= 1 && c <= g.pnx - 2) {
+                    ux = cf.c0x * (ur[c + 1] - ur[c]) + cf.c1x * (ur[c + 2] - ur[c - 1]);
+                } else if (c == 0) {                                      // fwi_2d.c:829
+                    ux = (ur[1] - ur[0]) * cf.ix;
+                } else if (c == g.pnx - 1) {                              // fwi_2d.c:831
+                    ux = (ur[g.pnx] - ur[g.pnx - 1]) * cf.ix;
+                } else {
+                    ux = 0.f;
+                }
+                if (row < g.pnz && c < g.pnx) {
+                    if (c < np) {                                         // fwi_2d.c:838-839
+                        const int idx = P.pl.ux0 + row * np + c;
+                        const float ps = b0x[2 * c + 1] * psr[idx] + a0x[2 * c + 1] * ux;
+                        psw[idx] = ps;
+                        ux += ps;
+                    } else if (c >= g.pnx - np) {                         // fwi_2d.c:841-842
+                        const int kk = c - (g.pnx - np);
+                        const int idx = P.pl.ux1 + row * np + kk;
+                        const float ps = b1x[2 * kk + 1] * psr[idx] + a1x[2 * kk + 1] * ux;
+                        psw[idx] = ps;
+                        ux += ps;
+                    }
+                    if (row >= g.pnz - np) {                              // fwi_2d.c:860-861
+                        const int kk = row - (g.pnz - np);
+                        const int idx = P.pl.vz1 + kk * g.pnx + c;
+                        const float ps = b1z[2 * kk + 1] * psr[idx] + a1z[2 * kk + 1] * vz;
+                        psw[idx] = ps;
+                        vz += ps;
+                    } else if (!g.fs && row < np) {
+                        const int idx = P.pl.vz0 + row * g.pnx + c;
+                        const float ps = b0z[2 * row + 1] * psr[idx] + a0z[2 * row + 1] * vz;
+                        psw[idx] = ps;
+                        vz += ps;
+                    }
+                }
+            }
+            float pn = 0.f;
+            if (!GEN || (row < g.pnz && c < g.pnx)) {
+                const long long o = (long long)row * g.ld + c;
+                const float kk = __ldg(K + o);
+                pn = fmaf(kk, ux + vz, fmaf(2.f, pc[i + 3], -pold[o]));      // fwi_2d.c:878
+                if (row == sd.src_r && c == sd.src_c) pn += amp * kk;
+                pold[o] = pn;
+                if (GEN) save_strip(P, sd, row, c, pn, P.step);
+            }
+            vals[h * R + i] = pn;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NTH) k_forward(const StepParams P)
+{
+    __shared__ __align__(16) float sp[SPH * SPW];
+    __shared__ __align__(16) float su[TZ * UWP];
+    const int s = blockIdx.z;
+    const ShotDev sd = P.shots[s];
+    if (P.step >= sd.nt) return;
+    const Geo& g = P.g;
+    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
+    const int tile = blockIdx.y * g.ntx + blockIdx.x;
+    stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
+    __syncthreads();
+    float vals[CX * R];
+    const bool gen = tile_general(g, x0, z0);
+    if (gen) fwd_tile<true>(P, sd, s, x0, z0, sp, su, vals);
+    else     fwd_tile<false>(P, sd, s, x0, z0, sp, su, vals);
+    if (!gen) {
+        // interior tiles can still hold strip cells when the CPML is thin
+        const int zs0 = g.z0p + NSTRIP, zs1 = g.z0p + g.nz - NSTRIP;
+        const int xs0 = g.x0p + NSTRIP, xs1 = g.x0p + g.nx - NSTRIP;
+        if (z0 < zs0 || z0 + TZ > zs1 || x0 < xs0 || x0 + TX > xs1) {
+            #pragma unroll
+            for (int h = 0; h < CX; ++h)
+                #pragma unroll
+                for (int i = 0; i < R; ++i)
+                    save_strip(P, sd, z0 + R * threadIdx.y + i, x0 + threadIdx.x + BX * h, vals[h * R + i], P.step);
+        }
+    }
+    // receiver sampling every jump steps (syn[r][k] = p^{k*jump+1})
+    const int rb = P.rtile[sd.rtile_off + tile], re = P.rtile[sd.rtile_off + tile + 1];
+    if (re > rb && (P.step % P.jump) == 0) {
+        __syncthreads();
+        #pragma unroll
+        for (int h = 0; h < CX; ++h)
+            #pragma unroll
+            for (int i = 0; i < R; ++i)
+                su[(R * threadIdx.y + i) * TX + threadIdx.x + BX * h] = vals[h * R + i];
+        __syncthreads();
+        const int k = P.step / P.jump;
+        for (int q = rb + threadIdx.y * BX + threadIdx.x; q < re; q += NTH) {
+            const RecDev rd = P.recs[q];
+            P.syn[rd.syn_base + k] = su[rd.cell];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Backward step: adjoint + rebuild + imaging
+// ---------------------------------------------------------------------------
+struct BwdSmem {
+    float sq[SPH * SPW];   // b^{m+1} tile + halo
+    float sp[SPH * SPW];   // p^{m-1} tile + halo
+    float su[TZ * UWP];    // adjoint ubar, then rebuild u
+    float srx[TZ * RXP];   // adjoint x-stage input (psi-adjusted b), general tiles
+    float racc[TZ * TX];   // receiver adjoint sources of the tile
+};
+
+template <bool GEN>
+__device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd, int s, int x0, int z0,
+                                         BwdSmem& sm, bool do_res, float* bm)
+{
+    const Geo& g = P.g;
+    const Coef& cf = P.c;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int np = g.npml, n2 = 2 * np + 1, pnx = g.pnx, pnz = g.pnz;
+    const long long so = (long long)s * g.fstride;
+    const float* __restrict__ psr = P.psr + (long long)s * P.pl.stride;
+    float* __restrict__ psw = P.psw + (long long)s * P.pl.stride;
+    const float* a0x = P.pmlc;          const float* b0x = a0x + n2;
+    const float* a1x = a0x + 2 * n2;    const float* b1x = a0x + 3 * n2;
+    const float* a0z = a0x + 4 * n2;    const float* b0z = a0x + 5 * n2;
+    const float* a1z = a0x + 6 * n2;    const float* b1z = a0x + 7 * n2;
+
+    // x stage 1 (general tiles): rbar = q adjusted by the adjoint of the ux psi recursion
+    if (GEN) {
+        #pragma unroll
+        for (int k = 0; k < R; ++k) {
+            const int rl = ty + BY * k, row = z0 + rl;
+            const float* qr = sm.sq + (rl + HZ) * SPW + HX - x0;
+            #pragma unroll
+            for (int h = 0; h < 3; ++h) {
+                const int ii = tx + BX * h;
+                if (ii >= RXW) break;
+                const int i = x0 - 3 + ii;
+                float r = qr[i];
+                if (row < pnz && i >= 0 && i < pnx) {
+                    const bool own = ii >= 3 && ii < 3 + TX;
+                    if (i < np) {
+                        const int idx = P.pl.ux0 + row * np + i;
+                        const float t = r + psr[idx];
+                        r = r + a0x[2 * i + 1] * t;
+                        if (own) psw[idx] = b0x[2 * i + 1] * t;
+                    } else if (i >= pnx - np) {
+                        const int kk = i - (pnx - np);
+                        const int idx = P.pl.ux1 + row * np + kk;
+                        const float t = r + psr[idx];
+                        r = r + a1x[2 * kk + 1] * t;
+                        if (own) psw[idx] = b1x[2 * kk + 1] * t;
+                    }
+                }
+                sm.srx[rl * RXP + ii] = r;
+            }
+        }
+        __syncthreads();
+    }
+    // x stage 2: ubar at u positions j in [x0-1, x0+TX+1]
+    #pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int rl = ty + BY * k, row = z0 + rl;
+        #pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            const int jj = tx + BX * h;
+            if (jj >= UW) break;
+            const int j = x0 - 1 + jj;
+            float ub;
+            if (!GEN) {
+                const float* qr = sm.sq + (rl + HZ) * SPW + HX - x0;
+                ub = cf.c0x * (qr[j - 1] - qr[j]) + cf.c1x * (qr[j - 2] - qr[j + 1]);
+            } else {
+                const float* rr = sm.srx + rl * RXP + 3 - x0;     // rr[i] = rbar[row][i]
+                #define RM(i) (((i) >= 1 && (i) <= pnx - 2) ? rr[i] : 0.f)
+                ub = cf.c0x * (RM(j - 1) - RM(j)) + cf.c1x * (RM(j - 2) - RM(j + 1));
+                #undef RM
+                if (j == 1) ub += cf.ix * rr[0];
+                if (j == 0) ub -= cf.ix * rr[0];
+                if (j == pnx) ub += cf.ix * rr[pnx - 1];
+                if (j == pnx - 1) ub -= cf.ix * rr[pnx - 1];
+                if (row < pnz) {
+                    const bool own = jj >= 1 && jj <= TX;
+                    if (j >= 0 && j <= np) {
+                        const int idx = P.pl.u0 + row * (np + 1) + j;
+                        const float t = ub + psr[idx];
+                        ub = ub + a0x[2 * j] * t;
+                        if (own) psw[idx] = b0x[2 * j] * t;
+                    } else if (j >= pnx - np && j <= pnx) {
+                        const int kk = j - (pnx - np);
+                        const int idx = P.pl.u1 + row * (np + 1) + kk;
+                        const float t = ub + psr[idx];
+                        ub = ub + a1x[2 * kk] * t;
+                        if (own) psw[idx] = b1x[2 * kk] * t;
+                    }
+                }
+            }
+            sm.su[rl * UWP + jj] = ub;
+        }
+    }
+    __syncthreads();
+
+    const int r0l = R * ty, r0 = z0 + r0l;
+    const float* __restrict__ K = P.K;
+    float* __restrict__ bold = P.bold + so;
+    #pragma unroll
+    for (int h = 0; h < CX; ++h) {
+        const int cl = tx + BX * h, c = x0 + cl;
+        float qc[R + 6];
+        #pragma unroll
+        for (int k = 0; k < R + 6; ++k) qc[k] = sm.sq[(r0l + k) * SPW + HX + cl];   // rows r0-3+k
+        float rz[R + 6];
+        #pragma unroll
+        for (int k = 0; k < R + 6; ++k) {
+            float r = qc[k];
+            if (GEN) {
+                const int row = r0 - 3 + k;
+                if (row >= 0 && row < pnz && c < pnx) {
+                    const bool own = k >= 3 && k < 3 + R;
+                    if (row >= pnz - np) {
+                        const int kk = row - (pnz - np);
+                        const int idx = P.pl.vz1 + kk * pnx + c;
+                        const float t = r + psr[idx];
+                        r = r + a1z[2 * kk + 1] * t;
+                        if (own) psw[idx] = b1z[2 * kk + 1] * t;
+                    } else if (!g.fs && row < np) {
+                        const int idx = P.pl.vz0 + row * pnx + c;
+                        const float t = r + psr[idx];
+                        r = r + a0z[2 * row + 1] * t;
+                        if (own) psw[idx] = b0z[2 * row + 1] * t;
+                    }
+                }
+            }
+            rz[k] = r;
+        }
+        float vb[R + 3];                                                  // vbar rows r0-1+k
+        #pragma unroll
+        for (int k = 0; k < R + 3; ++k) {
+            const int kv = r0 - 1 + k;
+            float v;
+            if (!GEN) {
+                v = cf.c0z * (rz[k + 1] - rz[k + 2]) + cf.c1z * (rz[k] - rz[k + 3]);
+            } else {
+                // rz index of row q is q - (r0 - 3); row kv-1 -> k+1 etc.
+                const float m1 = (kv - 1 >= 1 && kv - 1 <= pnz - 2) ? rz[k + 1] : 0.f;
+                const float m0 = (kv     >= 1 && kv     <= pnz - 2) ? rz[k + 2] : 0.f;
+                const float m2 = (kv - 2 >= 1 && kv - 2 <= pnz - 2) ? rz[k]     : 0.f;
+                const float p1 = (kv + 1 >= 1 && kv + 1 <= pnz - 2) ? rz[k + 3] : 0.f;
+                v = cf.c0z * (m1 - m0) + cf.c1z * (m2 - p1);
+                if (g.fs) {
+                    if (kv >= 0 && kv <= 4) {
+                        // vz[0] = (-22 v0 + 17 v1 + 9 v2 - 5 v3 + v4) iz24 (fwi_2d.c:848), transposed
+                        const float r00 = sm.sq[(HZ - z0) * SPW + HX + cl];   // rbar[0] = q[0] (no top CPML)
+                        const float hcoef = (kv == 0) ? -22.f : (kv == 1) ? 17.f : (kv == 2) ? 9.f : (kv == 3) ? -5.f : 1.f;
+                        v += hcoef * r00 * cf.iz24;
+                    }
+                } else {
+                    if (kv == 1) v += cf.iz * rz[3];      // r0 == 0 here: row 0 sits at index 3
+                    if (kv == 0) v -= cf.iz * rz[3];
+                }
+                if (kv == pnz) v += cf.iz * rz[k + 1];
+                if (kv == pnz - 1) v -= cf.iz * rz[k + 2];
+                if (c < pnx && kv >= 0 && kv <= pnz) {
+                    const bool own = k >= 1 && k <= R && kv < pnz;
+                    if (kv >= pnz - np) {
+                        const int kk = kv - (pnz - np);
+                        const int idx = P.pl.v1 + kk * pnx + c;
+                        const float t = v + psr[idx];
+                        v = v + a1z[2 * kk] * t;
+                        if (own) psw[idx] = b1z[2 * kk] * t;
+                    } else if (!g.fs && kv <= np) {
+                        const int idx = P.pl.v0 + kv * pnx + c;
+                        const float t = v + psr[idx];
+                        v = v + a0z[2 * kv] * t;
+                        if (own) psw[idx] = b0z[2 * kv] * t;
+                    }
+                }
+            }
+            vb[k] = v;
+        }
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int row = r0 + i;
+            const float* ub = sm.su + (r0l + i) * UWP + 1 - x0;              // ub[j] = ubar[row][j]
+            float pz, px;
+            if (!GEN) {
+                pz = cf.c0z * (vb[i + 1] - vb[i + 2]) + cf.c1z * (vb[i] - vb[i + 3]);
+                px = cf.c0x * (ub[c] - ub[c + 1]) + cf.c1x * (ub[c - 1] - ub[c + 2]);
+            } else {
+                // vbar index of row q is q - (r0 - 1)
+                const float M0 = (row     >= 2 && row     <= pnz - 2) ? vb[i + 1] : 0.f;
+                const float M1 = (row + 1 >= 2 && row + 1 <= pnz - 2) ? vb[i + 2] : 0.f;
+                const float Mm = (row - 1 >= 2 && row - 1 <= pnz - 2) ? vb[i]     : 0.f;
+                const float M2 = (row + 2 >= 2 && row + 2 <= pnz - 2) ? vb[i + 3] : 0.f;
+                pz = cf.c0z * (M0 - M1) + cf.c1z * (Mm - M2);
+                if (row >= 0 && row <= 3 && i == row) {                     // r0 == 0: vbar[0], vbar[1] at 1, 2
+                    if (g.fs) {
+                        const float g0 = (row == 0) ? 3675.f : (row == 1) ? -1225.f : (row == 2) ? 441.f : -75.f;
+                        const float g1 = (row == 0) ? -1085.f : (row == 1) ? 1015.f : (row == 2) ? -63.f : 5.f;
+                        pz += (g0 * vb[1] + g1 * vb[2]) * cf.iz840;
+                    } else {
+                        if (row == 1) pz += cf.iz * vb[2];
+                        if (row == 0) pz -= cf.iz * vb[2];
+                    }
+                }
+                if (row == pnz - 1) pz += cf.iz * vb[i + 1];
+                if (row == pnz - 2) pz -= cf.iz * vb[i + 2];
+                #define UM(j) (((j) >= 2 && (j) <= pnx - 2) ? ub[j] : 0.f)
+                px = cf.c0x * (UM(c) - UM(c + 1)) + cf.c1x * (UM(c - 1) - UM(c + 2));
+                #undef UM
+                if (c == 1) px += cf.ix * ub[1];
+                if (c == 0) px -= cf.ix * ub[1];
+                if (c == pnx - 1) px += cf.ix * ub[pnx - 1];
+                if (c == pnx - 2) px -= cf.ix * ub[pnx - 1];
+            }
+            float pbar = px + pz;
+            if (do_res) pbar += sm.racc[(r0l + i) * TX + cl];
+            float b = 0.f;
+            if (!GEN || (row < pnz && c < pnx)) {
+                const long long o = (long long)row * g.ld + c;
+                b = fmaf(__ldg(K + o), pbar, fmaf(2.f, qc[i + 3], -bold[o]));
+                bold[o] = b;
+            }
+            bm[h * R + i] = b;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
+    const int s = blockIdx.z;
+    const ShotDev sd = P.shots[s];
+    const int m = P.step;
+    if (m > sd.nt) return;
+    const Geo& g = P.g;
+    const Coef& cf = P.c;
+    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
+    const int tile = blockIdx.y * g.ntx + blockIdx.x;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
+    const long long so = (long long)s * g.fstride;
+
+    // physical region and the rebuilt interior (3 cells inside it)
+    const int zp0 = g.z0p, zp1 = g.z0p + g.nz, xp0 = g.x0p, xp1 = g.x0p + g.nx;
+    const bool phys = z0 < zp1 && z0 + TZ > zp0 && x0 < xp1 && x0 + TX > xp0;
+
+    stage_tile(P.bcur + so, g, x0, z0, sm.sq);
+    if (phys) stage_tile(P.pcur + so, g, x0, z0, sm.sp);
+
+    // adjoint sources r^m at the receivers when m-1 = k*jump
+    const int rb = P.rtile[sd.rtile_off + tile], re = P.rtile[sd.rtile_off + tile + 1];
+    const bool do_res = re > rb && ((m - 1) % P.jump) == 0;
+    if (do_res) {
+        for (int q = tid; q < TZ * TX; q += NTH) sm.racc[q] = 0.f;
+        __syncthreads();
+        const int k = (m - 1) / P.jump;
+        for (int q = rb + tid; q < re; q += NTH) {
+            const RecDev rd = P.recs[q];
+            atomicAdd(&sm.racc[rd.cell], P.res[rd.syn_base + k]);
+        }
+    }
+    __syncthreads();
+
+    float bm[CX * R];
+    if (tile_general(g, x0, z0)) adj_tile<true>(P, sd, s, x0, z0, sm, do_res, bm);
+    else                         adj_tile<false>(P, sd, s, x0, z0, sm, do_res, bm);
+    if (!phys) return;   // uniform per block
+
+    // rebuild of p^{m-2} and imaging
+    __syncthreads();     // su is reused
+    #pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int rl = ty + BY * k;
+        const float* pr = sm.sp + (rl + HZ) * SPW + HX - x0;
+        #pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            const int jj = tx + BX * h;
+            if (jj >= UW) break;
+            const int j = x0 - 1 + jj;
+            sm.su[rl * UWP + jj] = cf.c0x * (pr[j] - pr[j - 1]) + cf.c1x * (pr[j + 1] - pr[j - 2]);
+        }
+    }
+    __syncthreads();
+    const int r0l = R * ty, r0 = z0 + r0l;
+    const float* __restrict__ K = P.K;
+    float* __restrict__ pold = P.pold + so;
+    float* __restrict__ gacc = P.gacc + so;
+    const float f = P.wav[sd.wav_off + m - 1] * cf.iarea;
+    #pragma unroll
+    for (int h = 0; h < CX; ++h) {
+        const int cl = tx + BX * h, c = x0 + cl;
+        const int ix = c - g.x0p;
+        if (ix < 0 || ix >= g.nx) continue;
+        float pc[R + 6];
+        #pragma unroll
+        for (int k = 0; k < R + 6; ++k) pc[k] = sm.sp[(r0l + k) * SPW + HX + cl];
+        float vv[R + 3];
+        #pragma unroll
+        for (int k = 0; k < R + 3; ++k) vv[k] = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int row = r0 + i, iz = row - g.z0p;
+            if (iz < 0 || iz >= g.nz) continue;
+            const long long o = (long long)row * g.ld + c;
+            const float kk = __ldg(K + o);
+            const float pm = pold[o];            // p^m
+            const float p1 = pc[i + 3];          // p^{m-1}
+            float pn, lp;
+            if (iz >= NSTRIP && iz < g.nz - NSTRIP && ix >= NSTRIP && ix < g.nx - NSTRIP) {
+                const float* ur = sm.su + (r0l + i) * UWP + 1 - x0;
+                const float vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
+                const float ux = cf.c0x * (ur[c + 1] - ur[c]) + cf.c1x * (ur[c + 2] - ur[c - 1]);
+                const float w = ux + vz;
+                pn = fmaf(kk, w, fmaf(2.f, p1, -pm));
+                lp = w;
+                if (row == sd.src_r && c == sd.src_c) { pn += f * kk; lp += f; }
+            } else {
+                pn = (m - 3 >= 0) ? load_strip(P, sd, iz, ix, m - 3) : 0.f;
+                lp = ((pm - 2.f * p1) + pn) / kk;
+            }
+            pold[o] = pn;
+            gacc[o] = fmaf(bm[h * R + i], lp, gacc[o]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Misfit, model and reduction kernels
+// ---------------------------------------------------------------------------
+
+// K = vext^2 dt^2 with vext the edge-replicated model (model_ext /
+// model_ext_fs_no, fwi_2d.c:29-107, are clamp extensions).
+__global__ void k_build_K(const float* __restrict__ vel, float* __restrict__ K, Geo g, float dt)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y;
+    if (c >= g.pnx || r >= g.pnz) return;
+    const int iz = min(max(r - g.z0p, 0), g.nz - 1);
+    const int ix = min(max(c - g.x0p, 0), g.nx - 1);
+    const float v = vel[(long long)iz * g.nx + ix];
+    K[(long long)r * g.ld + c] = __fmul_rn(__fmul_rn(__fmul_rn(v, v), dt), dt);
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// res = syn - obs and per-block partial sums of res^2 (FP64).
+__global__ void k_misfit(const float* __restrict__ syn, const float* __restrict__ obs, float* __restrict__ res,
+                         long long n, double* __restrict__ partial)
+{
+    __shared__ double ws[32];
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float r = syn[i] - obs[i];
+        res[i] = r;
+        acc += (double)r * (double)r;
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) partial[blockIdx.x] = v;
+    }
+}
+
+// out[0] = out[1] = 1/2 sum partial (deterministic single-block sum).
+__global__ void k_misfit_final(const double* __restrict__ partial, int n, double* __restrict__ out)
+{
+    __shared__ double ws[32];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += partial[i];
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) { out[0] = 0.5 * v; out[1] = 0.5 * v; }
+    }
+}
+
+// grad[iz][ix] = 2 / v * sum_s g_s, summed in FP64 in shot order.
+__global__ void k_reduce(const float* __restrict__ gacc, const float* __restrict__ vel, double* __restrict__ grad,
+                         Geo g, int nshots)
+{
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iz = blockIdx.y;
+    if (ix >= g.nx || iz >= g.nz) return;
+    const long long o = (long long)(iz + g.z0p) * g.ld + ix + g.x0p;
+    double acc = 0.0;
+    for (int s = 0; s < nshots; ++s) acc += (double)gacc[(long long)s * g.fstride + o];
+    const long long q = (long long)iz * g.nx + ix;
+    grad[q] = 2.0 / (double)vel[q] * acc;
+}
+
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+}  // namespace fwi

@@ -1,0 +1,256 @@
+"""Python binding of the C ABI in ``include/fwi_gb300.h`` (ctypes).
+
+This is the host-side mirror used by the tests and the benchmark; C callers
+link ``libfwigpu.so`` directly.  Every method maps onto one ``fwi_*`` entry
+point and raises :class:`FwiError` with the library's status and message
+when the call fails.  Nothing here computes: if the library is missing or no
+sm_103 device is present the constructor raises instead of falling back.
+
+The call sequence mirrors one L-BFGS gradient evaluation of the reference
+(MBotOpt.c:98-99): broadcast the model, then every shot's ``grad4_1shot``
+(header.h:283) -- here one batched call over all shots.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libfwigpu.so")
+
+FWI_OK = 0
+STATUS = {0: "FWI_OK", -1: "FWI_ERR_ARG", -2: "FWI_ERR_GEOMETRY", -3: "FWI_ERR_NOMEM", -4: "FWI_ERR_CUDA",
+          -5: "FWI_ERR_STATE", -6: "FWI_ERR_CFL", -7: "FWI_ERR_NONFINITE", -8: "FWI_ERR_NODEVICE"}
+
+
+class FwiConfig(C.Structure):
+    _fields_ = [("nx", C.c_int), ("nz", C.c_int), ("dx", C.c_float), ("dz", C.c_float), ("dt", C.c_float),
+                ("nt_max", C.c_int), ("npml", C.c_int), ("free_surface", C.c_int), ("jump", C.c_int),
+                ("pml_max_f", C.c_float), ("pml_max_v", C.c_float), ("pml_coef_r", C.c_float),
+                ("device", C.c_int), ("use_graph", C.c_int), ("reserved", C.c_int * 7)]
+
+
+class FwiShot(C.Structure):
+    _fields_ = [("nt", C.c_int), ("nr", C.c_int), ("src_x", C.c_float), ("src_z", C.c_float),
+                ("rec_xz", C.POINTER(C.c_float)), ("wavelet", C.POINTER(C.c_float))]
+
+
+class FwiStats(C.Structure):
+    _fields_ = [("ms_forward", C.c_double), ("ms_backward", C.c_double), ("ms_misfit", C.c_double),
+                ("ms_reduce", C.c_double), ("cell_steps", C.c_double), ("launches", C.c_longlong),
+                ("device_bytes", C.c_longlong)]
+
+
+class FwiError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: {STATUS.get(status, status)}")
+
+
+_LIB = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load ``libfwigpu.so``; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.isfile(path):
+        raise FileNotFoundError(f"{path} is missing: run fwi2dacoustic-mpi-lbfgs_gb300/build.py "
+                                "(the engine has no CPU fallback)")
+    lib = C.CDLL(path)
+    P, I, F, D = C.c_void_p, C.c_int, C.c_float, C.c_double
+    lib.fwi_create.restype = P
+    lib.fwi_create.argtypes = [C.POINTER(FwiConfig), C.POINTER(I)]
+    lib.fwi_destroy.argtypes = [P]
+    lib.fwi_destroy.restype = None
+    lib.fwi_set_model.argtypes = [P, C.POINTER(F)]
+    lib.fwi_set_shots.argtypes = [P, I, C.POINTER(FwiShot)]
+    lib.fwi_set_observed.argtypes = [P, C.POINTER(F)]
+    lib.fwi_forward.argtypes = [P, C.POINTER(F)]
+    lib.fwi_backward.argtypes = [P, C.POINTER(F), C.POINTER(D)]
+    lib.fwi_gradient.argtypes = [P, C.POINTER(D), C.POINTER(D)]
+    lib.fwi_gradient_f32.argtypes = [P, C.POINTER(D), C.POINTER(F)]
+    lib.fwi_grad_device.argtypes = [P]
+    lib.fwi_grad_device.restype = P
+    lib.fwi_get_stats.argtypes = [P, C.POINTER(FwiStats)]
+    lib.fwi_status_string.argtypes = [I]
+    lib.fwi_status_string.restype = C.c_char_p
+    lib.fwi_last_error.argtypes = [P]
+    lib.fwi_last_error.restype = C.c_char_p
+    lib.fwi_check_config.argtypes = [C.POINTER(FwiConfig)]
+    lib.fwi_cpml_profile.argtypes = [I, F, F, F, F, F, C.POINTER(F), C.POINTER(F)]
+    lib.fwi_fd_coefficients.argtypes = [F, F, C.POINTER(F)]
+    lib.fwi_cell_of.argtypes = [F, F, F, F, C.POINTER(I), C.POINTER(I)]
+    _LIB = lib
+    return lib
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def make_config(nx, nz, dx, dz, dt, nt_max, npml=20, free_surface=1, jump=1, pml_max_f=15.0,
+                pml_max_v=6000.0, pml_coef_r=0.001, device=0, use_graph=0) -> FwiConfig:
+    """CPML defaults are MAX_F, MAX_V, COEF_R of fwi_sys.h:2-4."""
+    cfg = FwiConfig()
+    cfg.nx, cfg.nz, cfg.dx, cfg.dz, cfg.dt = nx, nz, dx, dz, dt
+    cfg.nt_max, cfg.npml, cfg.free_surface, cfg.jump = nt_max, npml, int(free_surface), jump
+    cfg.pml_max_f, cfg.pml_max_v, cfg.pml_coef_r = pml_max_f, pml_max_v, pml_coef_r
+    cfg.device, cfg.use_graph = device, use_graph
+    return cfg
+
+
+class ShotSpec:
+    """One shot in metres, as fwi_init reads it (sr_location file + wavelet)."""
+
+    def __init__(self, src_x, src_z, rec_xz, wavelet):
+        self.src_x, self.src_z = float(src_x), float(src_z)
+        self.rec_xz = np.ascontiguousarray(rec_xz, np.float32).reshape(-1, 2)
+        self.wavelet = np.ascontiguousarray(wavelet, np.float32)
+
+    @property
+    def nt(self):
+        return len(self.wavelet)
+
+    @property
+    def nr(self):
+        return len(self.rec_xz)
+
+    def nt0(self, jump):
+        return (self.nt - 1) // jump + 1
+
+
+class Engine:
+    """Owns one ``fwi_ctx``."""
+
+    def __init__(self, cfg: FwiConfig):
+        self.lib = load_library()
+        st = C.c_int(0)
+        self.cfg = cfg
+        self.ctx = self.lib.fwi_create(C.byref(cfg), C.byref(st))
+        if not self.ctx:
+            raise FwiError(st.value, "fwi_create")
+        self.shots: list[ShotSpec] = []
+        self._keep = None
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.fwi_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, what):
+        if st != FWI_OK:
+            msg = self.lib.fwi_last_error(self.ctx)
+            raise FwiError(st, f"{what} ({msg.decode() if msg else ''})")
+
+    @property
+    def nsamples(self):
+        return sum(s.nr * s.nt0(self.cfg.jump) for s in self.shots)
+
+    def set_model(self, vel):
+        vel = np.ascontiguousarray(vel, np.float32)
+        assert vel.shape == (self.cfg.nz, self.cfg.nx), vel.shape
+        self._check(self.lib.fwi_set_model(self.ctx, _fp(vel)), "fwi_set_model")
+
+    def set_shots(self, shots):
+        self.shots = list(shots)
+        arr = (FwiShot * len(self.shots))()
+        for a, s in zip(arr, self.shots):
+            a.nt, a.nr, a.src_x, a.src_z = s.nt, s.nr, s.src_x, s.src_z
+            a.rec_xz, a.wavelet = _fp(s.rec_xz), _fp(s.wavelet)
+        self._check(self.lib.fwi_set_shots(self.ctx, len(self.shots), arr), "fwi_set_shots")
+
+    def set_observed(self, obs):
+        obs = np.ascontiguousarray(obs, np.float32).ravel()
+        assert obs.size == self.nsamples, (obs.size, self.nsamples)
+        self._check(self.lib.fwi_set_observed(self.ctx, _fp(obs)), "fwi_set_observed")
+
+    def forward(self):
+        syn = np.zeros(self.nsamples, np.float32)
+        self._check(self.lib.fwi_forward(self.ctx, _fp(syn)), "fwi_forward")
+        return syn
+
+    def backward(self, residual):
+        res = np.ascontiguousarray(residual, np.float32).ravel()
+        grad = np.zeros((self.cfg.nz, self.cfg.nx), np.float64)
+        self._check(self.lib.fwi_backward(self.ctx, _fp(res), _dp(grad)), "fwi_backward")
+        return grad
+
+    def gradient(self, keep_on_device=False):
+        mis = np.zeros(2, np.float64)
+        grad = None if keep_on_device else np.zeros((self.cfg.nz, self.cfg.nx), np.float64)
+        self._check(self.lib.fwi_gradient(self.ctx, _dp(mis), _dp(grad)), "fwi_gradient")
+        return float(mis[1]), grad
+
+    def gradient_f32(self):
+        mis = np.zeros(2, np.float64)
+        grad = np.zeros((self.cfg.nz, self.cfg.nx), np.float32)
+        self._check(self.lib.fwi_gradient_f32(self.ctx, _dp(mis), _fp(grad)), "fwi_gradient_f32")
+        return float(mis[1]), grad
+
+    def stats(self) -> dict:
+        s = FwiStats()
+        self._check(self.lib.fwi_get_stats(self.ctx, C.byref(s)), "fwi_get_stats")
+        return {k: getattr(s, k) for k, _ in FwiStats._fields_}
+
+    def split(self, flat):
+        """Split a flat trace vector into per-shot [nr][nt0] arrays."""
+        out, o = [], 0
+        for s in self.shots:
+            n = s.nr * s.nt0(self.cfg.jump)
+            out.append(np.asarray(flat[o:o + n]).reshape(s.nr, s.nt0(self.cfg.jump)))
+            o += n
+        return out
+
+
+# ---- host-only helpers (no device needed) ----------------------------------------
+
+def cpml_profile(npml, d, dt, max_f=15.0, max_v=6000.0, coef_r=0.001):
+    lib = load_library()
+    a = np.zeros(2 * npml + 1, np.float32)
+    b = np.zeros(2 * npml + 1, np.float32)
+    st = lib.fwi_cpml_profile(npml, d, dt, max_f, max_v, coef_r, _fp(a), _fp(b))
+    if st:
+        raise FwiError(st, "fwi_cpml_profile")
+    return a, b
+
+
+def fd_coefficients(dx, dz):
+    lib = load_library()
+    out = np.zeros(8, np.float32)
+    st = lib.fwi_fd_coefficients(dx, dz, _fp(out))
+    if st:
+        raise FwiError(st, "fwi_fd_coefficients")
+    return out
+
+
+def cell_of(x, z, dx, dz):
+    lib = load_library()
+    ix, iz = C.c_int(), C.c_int()
+    st = lib.fwi_cell_of(x, z, dx, dz, C.byref(ix), C.byref(iz))
+    if st:
+        raise FwiError(st, "fwi_cell_of")
+    return ix.value, iz.value
+
+
+def check_config(cfg: FwiConfig) -> int:
+    return load_library().fwi_check_config(C.byref(cfg))

@@ -1,0 +1,152 @@
+/*
+ * fwi_gb300.h -- C ABI of the GB300 (sm_103a) engine for the FWI gradient
+ * hot path of FWI2DAcoustic-MPI-LBFGS.
+ *
+ * The reference's boundary is one collective call per MPI rank and shot,
+ *     void grad4_1shot(fwi_plan *plan, int iter);          header.h:283
+ * (called at MBotOpt.c:55 and MBotOpt.c:99, never defined in the reference),
+ * which reads the velocity model plan->model->md (fwi_2d.c:179, the L-BFGS x
+ * of MBotOpt.c:52), the observed traces plan->msf->obs0 (fwi_2d.c:196), the
+ * geometry plan->sou->{xyz_sr, wav0} (fwi_2d.c:217-220) and writes the
+ * gradient plan->grad->body (fwi_2d.c:380) and the misfit plan->msf->val
+ * (fwi_2d.c:207).  This header splits that call into a context holding the
+ * device state and a forward/backward pair, and batches all shots of an
+ * iteration on one GPU instead of one shot per MPI rank.
+ *
+ * Conventions: every function returns an FWI_* status (0 = success) and never
+ * exits; buffers are caller-owned host memory unless a name says _device;
+ * every call is ordered on the context's CUDA stream and has completed when
+ * it returns; a context is not thread safe.
+ *
+ * Discrete problem (identical to the CPU oracle):
+ *   p^{it+1} = 2 p^it - p^{it-1} + K (L p^it) + s^it,  K = v^2 dt^2,
+ *   L = the staggered 4th-order operator with CPML of a_lap_opt_2d_pml
+ *       (fwi_2d.c:761-864; all-sides CPML when free_surface == 0),
+ *   s^it = K(src) * wavelet[it] / (dx dz) at the source cell (fwi_2d.c:216),
+ *   syn[r][k] = p^{k*jump+1}(receiver r),  k = 0 .. nt0-1, nt0 = (nt-1)/jump+1,
+ *   J = 1/2 sum (syn - obs)^2,   gradient = dJ/dv on the physical grid
+ *       (exact discrete adjoint; CPML cells are not imaged).
+ */
+#ifndef FWI_GB300_H
+#define FWI_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define FWI_OK              0
+#define FWI_ERR_ARG        -1   /* bad argument or configuration            */
+#define FWI_ERR_GEOMETRY   -2   /* source/receiver outside the model        */
+#define FWI_ERR_NOMEM      -3   /* device or host allocation failed         */
+#define FWI_ERR_CUDA       -4   /* CUDA runtime error (see fwi_last_error)  */
+#define FWI_ERR_STATE      -5   /* call order (e.g. backward before forward) */
+#define FWI_ERR_CFL        -6   /* model violates the stability limit       */
+#define FWI_ERR_NONFINITE  -7   /* NaN/Inf in an input                      */
+#define FWI_ERR_NODEVICE   -8   /* no usable sm_103 device                  */
+
+/* ---- configuration ------------------------------------------------------ */
+typedef struct fwi_config {
+    int   nx, nz;          /* physical grid, model is [nz][nx], x fastest (fwi_2d.c:148) */
+    float dx, dz, dt;      /* metres, seconds (fwi_base, header.h:25) */
+    int   nt_max;          /* largest per-shot nt that fwi_set_shots may pass */
+    int   npml;            /* CPML cells (NPML, Mpar.h:16) */
+    int   free_surface;    /* 1: CPML left/right/bottom, top is a free surface
+                              (fwi_2d.c:154-157); 0: CPML on all four sides */
+    int   jump;            /* receiver sampling interval in steps (DAT_JUMP;
+                              (nt0-1)*jump == nt-1, fwi_2d.c:195) */
+    float pml_max_f;       /* MAX_F  (fwi_sys.h:2), e.g. 15 */
+    float pml_max_v;       /* MAX_V  (fwi_sys.h:3), e.g. 6000 */
+    float pml_coef_r;      /* COEF_R (fwi_sys.h:4), e.g. 0.001 */
+    int   device;          /* CUDA device ordinal */
+    int   use_graph;       /* 1: replay the time loops as one CUDA graph */
+    int   reserved[7];     /* must be zero */
+} fwi_config;
+
+/* One shot.  Positions are metres, converted to cells as fwi_init does:
+ * ix = round(x/dx), iz = round(z/dz - 0.5) (fwi_2d.c:363-371). */
+typedef struct fwi_shot {
+    int          nt;       /* time steps, 1 <= nt <= nt_max, (nt-1) % jump == 0 */
+    int          nr;       /* receivers (may differ between shots) */
+    float        src_x, src_z;
+    const float *rec_xz;   /* [nr][2] receiver (x, z), like sr_location files (fwi_2d.c:343) */
+    const float *wavelet;  /* [nt] source wavelet (sou->wav0, fwi_2d.c:352) */
+} fwi_shot;
+
+typedef struct fwi_stats {
+    double ms_forward;     /* device time of the last forward loop */
+    double ms_backward;    /* device time of the last backward loop */
+    double ms_misfit;      /* device time of the misfit/residual kernel */
+    double ms_reduce;      /* device time of the FP64 shot reduction */
+    double cell_steps;     /* physical cell-steps of the last gradient (x3 for fwd+rebuild+adjoint) */
+    long long launches;    /* kernels launched by the last gradient */
+    long long device_bytes;/* device memory held by the context */
+} fwi_stats;
+
+typedef struct fwi_ctx fwi_ctx;
+
+/* Creates the device context (replaces fwi_init's allocations, fwi_2d.c:139-396;
+ * the CPML profile follows cpml_coe, fwi_2d.c:110-137). */
+fwi_ctx *fwi_create(const fwi_config *cfg, int *status);
+void     fwi_destroy(fwi_ctx *ctx);
+
+/* Velocity model [nz][nx] (plan->model->md, MBotOpt.c:52/98).  Checks finiteness
+ * and the CFL limit; builds K = v^2 dt^2 on the padded grid (model_ext,
+ * fwi_2d.c:29-107). */
+int fwi_set_model(fwi_ctx *ctx, const float *vel);
+
+/* All shots of an iteration (one fwi_init per MPI rank in the reference,
+ * MBotOpt.c:51).  Allocates the per-shot device state. */
+int fwi_set_shots(fwi_ctx *ctx, int nshots, const fwi_shot *shots);
+
+/* Observed traces, all shots concatenated, shot s as [nr_s][nt0_s]
+ * (msf->obs0, fwi_2d.c:196, read at fwi_2d.c:342). */
+int fwi_set_observed(fwi_ctx *ctx, const float *obs);
+
+/* Forward half: models every shot, keeps the boundary strips for the
+ * backward half, and copies the traces to syn_out (layout of obs; NULL
+ * leaves them on the device). */
+int fwi_forward(fwi_ctx *ctx, float *syn_out);
+
+/* Backward half: given the adjoint sources residual (layout of obs; for the
+ * L2 misfit, syn - obs), back-propagates, images and reduces over shots in
+ * FP64.  grad_out [nz][nx] = dJ/dv.  Requires a preceding fwi_forward on the
+ * current model. */
+int fwi_backward(fwi_ctx *ctx, const float *residual, double *grad_out);
+
+/* Whole gradient on the device: forward, L2 misfit + residual (the missing
+ * L2norm of msf_pool.h:1 / Mpar.h:68), backward, FP64 reduction.
+ * misfit[0] = misfit[1] = 1/2 sum (syn - obs)^2 (msf->val[0..1],
+ * MBotOpt.c:61,88).  grad_out [nz][nx] host, or NULL to keep it on the device
+ * (fwi_grad_device). */
+int fwi_gradient(fwi_ctx *ctx, double *misfit, double *grad_out);
+
+/* Same as fwi_gradient, float gradient (plan->grad->body is float). */
+int fwi_gradient_f32(fwi_ctx *ctx, double *misfit, float *grad_out);
+
+/* Device pointer of the FP64 gradient [nz][nx] of the last backward pass. */
+const double *fwi_grad_device(const fwi_ctx *ctx);
+
+int fwi_get_stats(const fwi_ctx *ctx, fwi_stats *out);
+const char *fwi_status_string(int status);
+const char *fwi_last_error(const fwi_ctx *ctx);   /* detail of the last failure */
+int fwi_version(void);
+
+/* ---- host-only helpers (no device needed) ------------------------------ */
+/* Validates a configuration without touching a device. */
+int fwi_check_config(const fwi_config *cfg);
+/* CPML profile a, b on 2*npml+1 half-cell nodes; replaces cpml_coe
+ * (fwi_2d.c:110-137, header.h:227) with identical FP32 results. */
+int fwi_cpml_profile(int npml, float d, float dt, float max_f, float max_v, float coef_r,
+                     float *a, float *b);
+/* {c0x, c1x, 1/dx, c0z, c1z, 1/dz, 1/(840 dz), 1/(24 dz)} as fwi_2d.c:304-314. */
+int fwi_fd_coefficients(float dx, float dz, float *out8);
+/* Cell of a position in metres, as fwi_2d.c:363-364. */
+int fwi_cell_of(float x, float z, float dx, float dz, int *ix, int *iz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FWI_GB300_H */

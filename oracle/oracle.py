@@ -1,0 +1,283 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may import this module.  It loads
+
+* ``_build/libfwioracle_f32.so`` / ``_build/libfwioracle_f64.so`` -- the C
+  restatement of the reference's propagator kernels (fwi_2d.c) and of the
+  missing gradient driver ``grad4_1shot`` (header.h:283), FP32 and FP64 twins;
+* ``_ref/libfwiref.so`` (optional) -- the reference's own fwi_2d.c kernels
+  compiled from the reference checkout by ``make ref``; present only where the
+  reference sources are available.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REFDIR = os.path.join(HERE, "_ref")
+
+
+class OrcConfig(C.Structure):
+    _fields_ = [("nx", C.c_int), ("nz", C.c_int), ("npml", C.c_int),
+                ("free_surface", C.c_int), ("nt", C.c_int), ("jump", C.c_int),
+                ("dx", C.c_float), ("dz", C.c_float), ("dt", C.c_float),
+                ("pml_max_f", C.c_float), ("pml_max_v", C.c_float),
+                ("pml_coef_r", C.c_float), ("nthreads", C.c_int)]
+
+
+class OrcShot(C.Structure):
+    _fields_ = [("isx", C.c_int), ("isz", C.c_int), ("nr", C.c_int),
+                ("irx", C.POINTER(C.c_int)), ("irz", C.POINTER(C.c_int)),
+                ("wav", C.POINTER(C.c_float))]
+
+
+def build(ref_dir: str | None = None, quiet: bool = True) -> None:
+    """Compile the oracle twins (and the reference kernels when available)."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True, stdout=out)
+    ref_dir = ref_dir or "/root/reference"
+    if os.path.isfile(os.path.join(ref_dir, "fwi_2d.c")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_dir}"], check=True, stdout=out)
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype)) if a is not None else None
+
+
+def make_config(nx, nz, npml, nt, dx, dz, dt, free_surface=1, jump=1,
+                pml_max_f=15.0, pml_max_v=6000.0, pml_coef_r=0.001, nthreads=0) -> OrcConfig:
+    """Defaults of the CPML constants are fwi_sys.h:2-4 (MAX_F, MAX_V, COEF_R)."""
+    return OrcConfig(nx, nz, npml, int(free_surface), nt, jump, dx, dz, dt,
+                     pml_max_f, pml_max_v, pml_coef_r, nthreads)
+
+
+class Shot:
+    """Keeps the numpy buffers of one orc_shot alive."""
+
+    def __init__(self, isx, isz, irx, irz, wav):
+        self.irx = np.ascontiguousarray(irx, dtype=np.int32)
+        self.irz = np.ascontiguousarray(irz, dtype=np.int32)
+        self.wav = np.ascontiguousarray(wav, dtype=np.float32)
+        self.c = OrcShot(int(isx), int(isz), len(self.irx), _ptr(self.irx, C.c_int),
+                         _ptr(self.irz, C.c_int), _ptr(self.wav, C.c_float))
+
+    @property
+    def nr(self):
+        return len(self.irx)
+
+
+class Oracle:
+    """One twin of the restatement (``twin`` = 'f32' or 'f64')."""
+
+    def __init__(self, twin: str = "f32"):
+        path = os.path.join(BUILD, f"libfwioracle_{twin}.so")
+        if not os.path.isfile(path):
+            build()
+        self.lib = C.CDLL(path)
+        self.real = np.float32 if self.lib.orc_real_bytes() == 4 else np.float64
+        self.creal = C.c_float if self.real == np.float32 else C.c_double
+        self.twin = twin
+
+    # -- geometry -----------------------------------------------------------------
+    def grid(self, cfg):
+        out = (C.c_int * 4)()
+        self.lib.orc_grid(C.byref(cfg), out)
+        return tuple(out)  # pnx, pnz, x0, z0
+
+    def nt0(self, cfg):
+        return (cfg.nt - 1) // cfg.jump + 1
+
+    # -- single pieces ------------------------------------------------------------
+    def cpml_coe(self, npml, d, dt, max_f=15.0, max_v=6000.0, coef_r=0.001):
+        a = np.zeros(2 * npml + 1, np.float32)
+        b = np.zeros(2 * npml + 1, np.float32)
+        self.lib.orc_cpml_coe(_ptr(a, C.c_float), _ptr(b, C.c_float), C.c_int(npml), C.c_float(d),
+                              C.c_float(dt), C.c_float(max_f), C.c_float(max_v), C.c_float(coef_r))
+        return a, b
+
+    def model_ext(self, model, en1, en2, fs):
+        model = np.ascontiguousarray(model, np.float32)
+        n2, n1 = model.shape
+        out = np.zeros((en2, en1), np.float32)
+        self.lib.orc_model_ext(_ptr(model, C.c_float), n1, n2, _ptr(out, C.c_float), en1, en2, int(fs))
+        return out
+
+    def fd_coeffs(self, dx, dz):
+        out = np.zeros(8, np.float32)
+        self.lib.orc_fd_coeffs(C.c_float(dx), C.c_float(dz), _ptr(out, C.c_float))
+        return out
+
+    def ekp(self, cfg, vel):
+        pnx, pnz, _, _ = self.grid(cfg)
+        vel = np.ascontiguousarray(vel, np.float32)
+        out = np.zeros((pnz, pnx), np.float32)
+        self.lib.orc_ekp(C.byref(cfg), _ptr(vel, C.c_float), _ptr(out, C.c_float))
+        return out
+
+    def psi_len(self, cfg):
+        return self.lib.orc_psi_len(C.byref(cfg))
+
+    def apply_op(self, cfg, p, psi):
+        pnx, pnz, _, _ = self.grid(cfg)
+        p = np.ascontiguousarray(p, self.real)
+        psi = np.ascontiguousarray(psi, self.real).copy()
+        w = np.zeros((pnz, pnx), self.real)
+        st = self.lib.orc_apply_op(C.byref(cfg), _ptr(p, self.creal), _ptr(psi, self.creal), _ptr(w, self.creal))
+        assert st == 0, st
+        return w, psi
+
+    def apply_op_t(self, cfg, q, psib):
+        pnx, pnz, _, _ = self.grid(cfg)
+        q = np.ascontiguousarray(q, self.real)
+        psib = np.ascontiguousarray(psib, self.real).copy()
+        pbar = np.zeros((pnz, pnx), self.real)
+        st = self.lib.orc_apply_op_t(C.byref(cfg), _ptr(q, self.creal), _ptr(psib, self.creal),
+                                     _ptr(pbar, self.creal))
+        assert st == 0, st
+        return pbar, psib
+
+    def apply_int(self, cfg, p):
+        p = np.ascontiguousarray(p, self.real)
+        ux = np.zeros_like(p)
+        vz = np.zeros_like(p)
+        assert self.lib.orc_apply_int(C.byref(cfg), _ptr(p, self.creal), _ptr(ux, self.creal),
+                                      _ptr(vz, self.creal)) == 0
+        return ux, vz
+
+    def strips_write(self, cfg, p_pad):
+        p_pad = np.ascontiguousarray(p_pad, self.real)
+        ud = np.zeros((6, cfg.nx), self.real)
+        lr = np.zeros((cfg.nz, 6), self.real)
+        self.lib.orc_strips_write(C.byref(cfg), _ptr(p_pad, self.creal), _ptr(ud, self.creal),
+                                  _ptr(lr, self.creal))
+        return ud, lr
+
+    # -- drivers ------------------------------------------------------------------
+    def forward(self, cfg, vel, shot: Shot, finals=False):
+        pnx, pnz, _, _ = self.grid(cfg)
+        vel = np.ascontiguousarray(vel, np.float32)
+        syn = np.zeros((shot.nr, self.nt0(cfg)), self.real)
+        pf = np.zeros((pnz, pnx), self.real) if finals else None
+        pp = np.zeros((pnz, pnx), self.real) if finals else None
+        st = self.lib.orc_forward(C.byref(cfg), _ptr(vel, C.c_float), C.byref(shot.c), _ptr(syn, self.creal),
+                                  _ptr(pf, self.creal), _ptr(pp, self.creal))
+        if st:
+            raise ValueError(f"orc_forward failed: {st}")
+        return (syn, pf, pp) if finals else syn
+
+    def gradient(self, cfg, vel, shots, obs_list):
+        vel = np.ascontiguousarray(vel, np.float32)
+        arr = (OrcShot * len(shots))(*[s.c for s in shots])
+        obs = np.ascontiguousarray(np.concatenate([np.asarray(o, np.float32).ravel() for o in obs_list]))
+        syn = np.zeros(obs.size, self.real)
+        grad = np.zeros((cfg.nz, cfg.nx), np.float64)
+        mis = np.zeros(1, np.float64)
+        st = self.lib.orc_gradient(C.byref(cfg), _ptr(vel, C.c_float), len(shots), arr, _ptr(obs, C.c_float),
+                                   _ptr(mis, C.c_double), _ptr(grad, C.c_double), _ptr(syn, self.creal))
+        if st:
+            raise ValueError(f"orc_gradient failed: {st}")
+        return float(mis[0]), grad, syn
+
+    def backward(self, cfg, vel, shot, res):
+        vel = np.ascontiguousarray(vel, np.float32)
+        res = np.ascontiguousarray(res, self.real)
+        grad = np.zeros((cfg.nz, cfg.nx), np.float64)
+        st = self.lib.orc_backward(C.byref(cfg), _ptr(vel, C.c_float), C.byref(shot.c), _ptr(res, self.creal),
+                                   _ptr(grad, C.c_double))
+        if st:
+            raise ValueError(f"orc_backward failed: {st}")
+        return grad
+
+    def adjoint_wavelet(self, cfg, vel, shot, res):
+        vel = np.ascontiguousarray(vel, np.float32)
+        res = np.ascontiguousarray(res, self.real)
+        wbar = np.zeros(cfg.nt, self.real)
+        st = self.lib.orc_adjoint_wavelet(C.byref(cfg), _ptr(vel, C.c_float), C.byref(shot.c),
+                                          _ptr(res, self.creal), _ptr(wbar, self.creal))
+        if st:
+            raise ValueError(f"orc_adjoint_wavelet failed: {st}")
+        return wbar
+
+    def probe(self, cfg, vel, shot, steps, fwd=True, reb=True):
+        pnx, pnz, _, _ = self.grid(cfg)
+        vel = np.ascontiguousarray(vel, np.float32)
+        steps = np.ascontiguousarray(steps, np.int32)
+        fs = np.zeros((len(steps), pnz, pnx), self.real) if fwd else None
+        rs = np.zeros((len(steps), cfg.nz, cfg.nx), self.real) if reb else None
+        st = self.lib.orc_probe(C.byref(cfg), _ptr(vel, C.c_float), C.byref(shot.c), len(steps),
+                                _ptr(steps, C.c_int), _ptr(fs, self.creal), _ptr(rs, self.creal))
+        if st:
+            raise ValueError(f"orc_probe failed: {st}")
+        return fs, rs
+
+
+class RefKernels:
+    """The reference's own kernels (oracle/_ref/libfwiref.so), FP32."""
+
+    path = os.path.join(REFDIR, "libfwiref.so")
+
+    @classmethod
+    def available(cls) -> bool:
+        return os.path.isfile(cls.path)
+
+    def __init__(self):
+        self.lib = C.CDLL(self.path)
+
+    def cpml_coe(self, npml, d, dt, max_f=15.0, max_v=6000.0, coef_r=0.001):
+        a = np.zeros(2 * npml + 1, np.float32)
+        b = np.zeros(2 * npml + 1, np.float32)
+        self.lib.ref_cpml_coe(_ptr(a, C.c_float), _ptr(b, C.c_float), C.c_int(npml), C.c_float(d),
+                              C.c_float(dt), C.c_float(max_f), C.c_float(max_v), C.c_float(coef_r))
+        return a, b
+
+    def model_ext(self, model, en1, en2, fs):
+        model = np.ascontiguousarray(model, np.float32)
+        n2, n1 = model.shape
+        out = np.zeros((en2, en1), np.float32)
+        self.lib.ref_model_ext(_ptr(model, C.c_float), n1, n2, _ptr(out, C.c_float), en1, en2, int(fs))
+        return out
+
+    def apply_op(self, cfg, p, psi):
+        p = np.ascontiguousarray(p, np.float32)
+        psi = np.ascontiguousarray(psi, np.float32).copy()
+        w = np.zeros_like(p)
+        assert self.lib.ref_apply_op(C.byref(cfg), _ptr(p, C.c_float), _ptr(psi, C.c_float), _ptr(w, C.c_float)) == 0
+        return w, psi
+
+    def apply_int(self, cfg, p):
+        p = np.ascontiguousarray(p, np.float32)
+        ux = np.zeros_like(p)
+        vz = np.zeros_like(p)
+        assert self.lib.ref_apply_int(C.byref(cfg), _ptr(p, C.c_float), _ptr(ux, C.c_float), _ptr(vz, C.c_float)) == 0
+        return ux, vz
+
+    def strips_write(self, cfg, p_pad):
+        p_pad = np.ascontiguousarray(p_pad, np.float32)
+        ud = np.zeros((6, cfg.nx), np.float32)
+        lr = np.zeros((cfg.nz, 6), np.float32)
+        self.lib.ref_strips_write(C.byref(cfg), _ptr(p_pad, C.c_float), _ptr(ud, C.c_float), _ptr(lr, C.c_float))
+        return ud, lr
+
+    def forward(self, cfg, vel, shot: Shot, nt_mem, steps=()):
+        pnx = cfg.nx + 2 * cfg.npml
+        pnz = cfg.nz + (1 if cfg.free_surface else 2) * cfg.npml
+        nt0 = (cfg.nt - 1) // cfg.jump + 1
+        vel = np.ascontiguousarray(vel, np.float32)
+        syn = np.zeros((shot.nr, nt0), np.float32)
+        pf = np.zeros((pnz, pnx), np.float32)
+        pp = np.zeros((pnz, pnx), np.float32)
+        steps = np.ascontiguousarray(steps, np.int32)
+        fs = np.zeros((len(steps), pnz, pnx), np.float32)
+        rs = np.zeros((len(steps), cfg.nz, cfg.nx), np.float32)
+        st = self.lib.ref_forward(C.byref(cfg), _ptr(vel, C.c_float), C.byref(shot.c), int(nt_mem),
+                                  _ptr(syn, C.c_float), _ptr(pf, C.c_float), _ptr(pp, C.c_float),
+                                  len(steps), _ptr(steps, C.c_int), _ptr(fs, C.c_float), _ptr(rs, C.c_float))
+        if st:
+            raise ValueError(f"ref_forward failed: {st}")
+        return syn, pf, pp, fs, rs

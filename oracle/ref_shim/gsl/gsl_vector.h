@@ -1,0 +1,1 @@
+/* Empty stand-in: the propagator files use no GSL symbol. */
