@@ -1,0 +1,384 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched FWI gradient on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one full gradient of the shot batch of the workload (default: the
+560 x 1700 grid, nt 4000, 64 shots, 1700 receivers): forward modelling with
+strip saving, L2 misfit and residual, exact adjoint with source rebuild and
+imaging, and the FP64 reduction over shots.  Prints one JSON line.
+
+* ``value``: shot-gradients/s over the whole job with every input resident in
+  HBM (CUDA events on the engine's stream, W warm-up steps, K timed steps).
+* ``e2e``: the same metric through the C ABI with host buffers: every step
+  uploads the model and the observed traces from pinned memory and reads back
+  the misfit and the FP64 gradient.
+* ``roofline``: the dominant kernel (the fused backward step) at its
+  algorithmic 36 B per physical cell-step against the measured HBM copy peak.
+* ``cpu_baseline``: the CPU port of the reference path (oracle/, all host
+  cores) on a bounded sample of the same workload, extrapolated; the same
+  sample checks the GPU gradient against the FP64 oracle.
+
+``--impl reference`` times only the CPU path (the reference's own algorithm,
+restated in oracle/ because the reference's gradient driver does not exist
+and its sources are not on the GPU host) on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fwi2dacoustic-mpi-lbfgs_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "shot-gradients/s & Gcell-steps/s, batched vs plain, at ≤1e-4 grad rel err"
+UNIT = "shot-gradients/s"
+BWD_BYTES = 36.0   # algorithmic bytes per physical cell-step of the fused backward step
+FWD_BYTES = 16.0   # ... of the forward step
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--nshots", type=int, default=None)
+    ap.add_argument("--nt", type=int, default=None)
+    ap.add_argument("--plain-shots", type=int, default=4)
+    ap.add_argument("--cpu-steps", type=int, default=2000, help="time steps of the CPU sample")
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--skip", default="", help="comma list of: e2e,plain,cpu")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi every 200 ms while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(device)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(5)
+            except Exception:
+                self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def traffic_per_cell_step(kernel):
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return float(json.load(f)[kernel]["dram_bytes_per_cell_step"])
+    except Exception:
+        return None
+
+
+def workload(args):
+    import workloads
+    return workloads.build(args.workload, scale=args.scale, nshots=args.nshots, nt=args.nt)
+
+
+def describe(args, cfgkw, shots):
+    nts = sorted({s.nt for s in shots})
+    nrs = sorted({s.nr for s in shots})
+    return {"workload": f"{args.workload}: {cfgkw['nz']}x{cfgkw['nx']} grid, dx {cfgkw['dx']} m, "
+                        f"dt {cfgkw['dt'] * 1e3:g} ms, CPML {cfgkw['npml']}, {len(shots)} shots",
+            "nz": cfgkw["nz"], "nx": cfgkw["nx"], "npml": cfgkw["npml"], "shots": len(shots),
+            "nt": nts[0] if len(nts) == 1 else [nts[0], nts[-1]],
+            "receivers": nrs[0] if len(nrs) == 1 else [nrs[0], nrs[-1]],
+            "fd_order": 4, "free_surface": True, "checkpointing": "boundary strips in HBM",
+            "l2": "working set larger than L2 (no flush)", "parallelism": f"shots batched per launch",
+            "data": "synthetic seeded model and acquisition; observed traces modelled on the true model"}
+
+
+def cpu_sample(args, cfgkw, vstart, vtrue, shot, check_gpu=None):
+    """Times the CPU port (oracle/, FP32, all host cores) on one shot and the
+    first args.cpu_steps time steps; optionally checks a GPU gradient of the
+    same sample against the FP64 oracle."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle as O
+    import build as engine_build
+    O.build()
+    engine_build.build()        # host helpers of the engine library (cell rounding)
+    nt = min(args.cpu_steps, shot.nt)
+    nt = (nt - 1) // cfgkw["jump"] * cfgkw["jump"] + 1
+    cores = os.cpu_count() or 1
+    ocfg = O.make_config(nx=cfgkw["nx"], nz=cfgkw["nz"], npml=cfgkw["npml"], nt=nt, dx=cfgkw["dx"],
+                         dz=cfgkw["dz"], dt=cfgkw["dt"], free_surface=1, jump=cfgkw["jump"], nthreads=cores)
+    import fwigpu
+    dx, dz = cfgkw["dx"], cfgkw["dz"]
+    isx, isz = fwigpu.cell_of(shot.src_x, shot.src_z, dx, dz)     # fwi_2d.c:363-364 rounding
+    cells = [fwigpu.cell_of(float(x), float(z), dx, dz) for x, z in shot.rec_xz]
+    irx = np.array([c[0] for c in cells], np.int32)
+    irz = np.array([c[1] for c in cells], np.int32)
+    osh = O.Shot(isx, isz, irx, irz, shot.wavelet[:nt])
+    o32 = O.Oracle("f32")
+    obs = o32.forward(ocfg, vtrue, osh).astype(np.float32)
+    t0 = time.perf_counter()
+    J32, g32, _ = o32.gradient(ocfg, vstart, [osh], [obs])
+    sec = time.perf_counter() - t0
+    out = {"sec": sec, "nt": nt, "cores": cores, "obs": obs, "g32": g32}
+    if check_gpu is not None:
+        o64 = O.Oracle("f64")
+        J64, g64, _ = o64.gradient(ocfg, vstart, [osh], [obs])
+        g_gpu = check_gpu(nt, obs)
+        out["grad_rel_err"] = float(np.linalg.norm(g_gpu - g64) / np.linalg.norm(g64))
+        out["grad_rel_err_cpu_fp32"] = float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))
+    return out
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cfgkw, vtrue, vstart, shots = workload(args)
+    nshots = len(shots)
+    times = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(args, cfgkw, vstart, vtrue, shots[0])
+        if i >= args.warmup:
+            times.append(r["sec"])
+    sec_shot = statistics.median(times) * shots[0].nt / r["nt"]         # linear in steps
+    ms_step = sec_shot * nshots * 1e3
+    value = nshots / (ms_step / 1e3)
+    sample = (f"1 shot of the workload, first {r['nt']} of {shots[0].nt} steps (forward, misfit, adjoint, "
+              f"rebuild, imaging; FP32), extrapolated linearly to {nshots} full shots")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": describe(args, cfgkw, shots),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    skip = set(filter(None, args.skip.split(",")))
+    import build as engine_build
+    if rank == 0:
+        engine_build.build()
+    if dist:
+        dist.barrier()
+    import fwigpu
+
+    cfgkw, vtrue, vstart, shots = workload(args)
+    nshots = len(shots)
+    cfg = fwigpu.make_config(**cfgkw, device=local, use_graph=0 if args.no_graph else 1)
+    eng = fwigpu.Engine(cfg)
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream.cuda_stream)
+    eng.set_shots(shots)
+    eng.set_model(vtrue)
+    obs = eng.forward()                      # observed traces from the true model (setup, untimed)
+    eng.set_observed(obs)
+    eng.set_model(vstart)
+    cells = float(cfgkw["nx"] * cfgkw["nz"])
+    step_cells = sum(s.nt for s in shots) * cells          # physical cell-steps of one propagation pass
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    grad_t = None
+    if dist:
+        # the gradient lives in the engine; all ranks sum their shot partitions in FP64
+        class _View:
+            def __init__(self, ptr, n):
+                self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 2}
+        grad_t = torch.as_tensor(_View(eng.grad_device_ptr(), int(cells)), device=f"cuda:{local}")
+
+    def step():
+        J, _ = eng.gradient(keep_on_device=True)
+        if dist:
+            with torch.cuda.stream(stream):
+                dist.all_reduce(grad_t)
+        return J
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    barrier()
+    clk = Clocks(local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fwd_ms = bwd_ms = 0.0
+    launches = 0
+    for _ in range(args.steps):
+        step()
+        st = eng.stats()
+        fwd_ms += st["ms_forward"]
+        bwd_ms += st["ms_backward"]
+        launches += st["launches"]
+    e1.record(stream)
+    barrier()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nshots / (ms / 1e3)
+    gcell = world * 3.0 * step_cells / (ms / 1e3) / 1e9
+
+    # roofline of the dominant kernel (fused backward step), per launch
+    nt_max = max(s.nt for s in shots)
+    bwd_launch_ms = bwd_ms / args.steps / nt_max
+    bwd_bytes_launch = BWD_BYTES * step_cells / nt_max                   # average over launches
+    peak, peak_kind = peaks()
+    achieved = bwd_bytes_launch / (bwd_launch_ms / 1e3) / 1e9
+    tpc = traffic_per_cell_step("k_backward")
+    roof = {"kernel": "k_backward", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": peak_kind,
+            "traffic": (tpc * step_cells / nt_max) if tpc else None,
+            "algorithmic_bytes_per_launch": bwd_bytes_launch, "avg_launch_ms": bwd_launch_ms,
+            "forward_avg_launch_ms": fwd_ms / args.steps / nt_max,
+            "forward_achieved_gbs": FWD_BYTES * step_cells / nt_max / (fwd_ms / args.steps / nt_max / 1e3) / 1e9}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": describe(args, cfgkw, shots),
+            "gcell_steps_per_s": gcell, "gpu_launches": launches, "clocks": clocks, "roofline": roof}
+
+    # end to end through the C ABI with pinned host buffers
+    if "e2e" not in skip:
+        v_h = torch.empty(vstart.shape, dtype=torch.float32, pin_memory=True).numpy()
+        v_h[:] = vstart
+        o_h = torch.empty(obs.shape, dtype=torch.float32, pin_memory=True).numpy()
+        o_h[:] = obs
+        g_h = torch.empty(vstart.shape, dtype=torch.float64, pin_memory=True).numpy()
+
+        def e2e_step():
+            eng.set_model(v_h)
+            eng.set_observed(o_h)
+            eng.gradient(out=g_h)
+            if dist:
+                gt = torch.from_numpy(g_h)
+                dist.all_reduce(gt.cuda())
+        e2e_step()
+        barrier()
+        k2 = max(1, min(args.steps, 3))
+        e0.record(stream)
+        for _ in range(k2):
+            e2e_step()
+        e1.record(stream)
+        barrier()
+        ms2 = e0.elapsed_time(e1) / k2
+        line["e2e"] = {"value": world * nshots / (ms2 / 1e3), "unit": UNIT, "ms_per_step": ms2,
+                       "h2d_bytes_per_step": int(v_h.nbytes + o_h.nbytes), "d2h_bytes_per_step": int(g_h.nbytes + 16)}
+
+    # plain per-shot path (one shot per launch, shots one after another)
+    if "plain" not in skip and rank == 0:
+        k = min(args.plain_shots, nshots)
+        pcfg = fwigpu.make_config(**dict(cfgkw, nt_max=max(s.nt for s in shots[:k])), device=local,
+                                  use_graph=0, plain_per_shot=1)
+        with fwigpu.Engine(pcfg) as pe:
+            pe.set_stream(stream.cuda_stream)
+            pe.set_shots(shots[:k])
+            pe.set_model(vstart)
+            pe.set_observed(obs[:pe.nsamples])
+            pe.gradient(keep_on_device=True)
+            e0.record(stream)
+            pe.gradient(keep_on_device=True)
+            e1.record(stream)
+            barrier()
+            pms = e0.elapsed_time(e1)
+        line["plain"] = {"shots": k, "value": k / (pms / 1e3), "unit": UNIT,
+                         "batched_over_plain": value / world / (k / (pms / 1e3))}
+
+    # CPU baseline (the reference's path restated in oracle/) and the accuracy check
+    if "cpu" not in skip and rank == 0 and world == 1:
+        def gpu_grad(nt, obs_sample):
+            import fwigpu as F
+            s0 = shots[0]
+            sh = F.ShotSpec(s0.src_x, s0.src_z, s0.rec_xz, s0.wavelet[:nt])
+            c1 = F.make_config(**dict(cfgkw, nt_max=nt), device=local)
+            with F.Engine(c1) as e1_:
+                e1_.set_shots([sh])
+                e1_.set_model(vstart)
+                e1_.set_observed(obs_sample)
+                return e1_.gradient()[1]
+        r = cpu_sample(args, cfgkw, vstart, vtrue, shots[0], check_gpu=gpu_grad)
+        sec_shot = r["sec"] * shots[0].nt / r["nt"]
+        line["cpu_baseline"] = {"value": 1.0 / sec_shot, "unit": UNIT, "cores": r["cores"], "kind": "port",
+                                "sample": f"1 shot, first {r['nt']} of {shots[0].nt} steps, FP32, "
+                                          f"{r['sec']:.2f} s, extrapolated linearly in steps"}
+        line["accuracy"] = {"grad_rel_err_vs_fp64": r["grad_rel_err"],
+                            "cpu_fp32_grad_rel_err_vs_fp64": r["grad_rel_err_cpu_fp32"],
+                            "sample": f"1 shot, {r['nt']} steps, workload grid"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

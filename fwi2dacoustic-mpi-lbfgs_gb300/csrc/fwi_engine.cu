@@ -66,8 +66,12 @@ inline void cell_of(float x, float z, float dx, float dz, int* ix, int* iz)
 
 struct fwi_ctx {
     fwi_config cfg{};
-    cudaStream_t st = nullptr;
-    cudaEvent_t ev[6]{};
+    cudaStream_t own = nullptr;    // the context's stream
+    cudaStream_t st = nullptr;     // stream in use (own, or the caller's)
+    cudaEvent_t ev[8]{};           // [0,1] forward, [2,3] backward, [4,5] misfit, [6,7] whole call
+    cudaGraph_t graph[3]{};        // captured phases (use_graph): forward, misfit, backward
+    cudaGraphExec_t gexec[3]{};
+    long long graph_launches[3]{};
     Geo g{};
     Coef c{};
     PsiLayout pl{};
@@ -138,8 +142,19 @@ int dalloc(fwi_ctx* x, T** p, size_t n, size_t* acc)
     return FWI_OK;
 }
 
+void drop_graph(fwi_ctx* x)
+{
+    for (int i = 0; i < 3; ++i) {
+        if (x->gexec[i]) cudaGraphExecDestroy(x->gexec[i]);
+        if (x->graph[i]) cudaGraphDestroy(x->graph[i]);
+        x->gexec[i] = nullptr;
+        x->graph[i] = nullptr;
+    }
+}
+
 void free_shots(fwi_ctx* x)
 {
+    drop_graph(x);
     void* ps[] = {x->F, x->A, x->Gacc, x->psiF, x->psiA, x->ring, x->syn, x->res, x->obs, x->wav,
                   x->shots_d, x->recs_d, x->rtile_d, x->partial, x->mis};
     for (void* p : ps) if (p) cudaFree(p);
@@ -185,31 +200,33 @@ int run_forward(fwi_ctx* x)
     CK(cudaMemsetAsync(x->psiF, 0, sizeof(float) * 2 * phalf, x->st));
     StepParams P = base_params(x);
     const dim3 block(BX, BY);
-    CK(cudaEventRecord(x->ev[0], x->st));
     long long launches = 0;
-    for (int it = 0; it < x->nt_run; ++it) {
-        const int nact = active_slots(x, it + 1);
-        P.step = it;
-        P.pcur = x->F + (long long)(it & 1) * half + x->origin;
-        P.pold = x->F + (long long)((it + 1) & 1) * half + x->origin;
-        P.psr = x->psiF + (long long)(it & 1) * phalf;
-        P.psw = x->psiF + (long long)((it + 1) & 1) * phalf;
-        k_forward<<<dim3(x->g.ntx, x->g.ntz, nact), block, 0, x->st>>>(P);
-        ++launches;
+    // batched: one launch per step over the active shots; plain: shot after shot
+    const int groups = x->cfg.plain_per_shot ? x->nshots : 1;
+    for (int grp = 0; grp < groups; ++grp) {
+        const int nt_grp = x->cfg.plain_per_shot ? x->nt_slot[grp] : x->nt_run;
+        for (int it = 0; it < nt_grp; ++it) {
+            const int nact = x->cfg.plain_per_shot ? 1 : active_slots(x, it + 1);
+            P.shot_base = x->cfg.plain_per_shot ? grp : 0;
+            P.step = it;
+            P.pcur = x->F + (long long)(it & 1) * half + x->origin;
+            P.pold = x->F + (long long)((it + 1) & 1) * half + x->origin;
+            P.psr = x->psiF + (long long)(it & 1) * phalf;
+            P.psw = x->psiF + (long long)((it + 1) & 1) * phalf;
+            k_forward<<<dim3(x->g.ntx, x->g.ntz, nact), block, 0, x->st>>>(P);
+            ++launches;
+        }
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(x->ev[1], x->st));
     x->stats.launches = launches;
     return FWI_OK;
 }
 
 int run_misfit(fwi_ctx* x)
 {
-    CK(cudaEventRecord(x->ev[4], x->st));
     k_misfit<<<x->npartial, 256, 0, x->st>>>(x->syn, x->obs, x->res, x->nsamples, x->partial);
     k_misfit_final<<<1, 256, 0, x->st>>>(x->partial, x->npartial, x->mis);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(x->ev[5], x->st));
     x->stats.launches += 2;
     return FWI_OK;
 }
@@ -225,22 +242,25 @@ int run_backward(fwi_ctx* x)
     P.gacc = x->Gacc + x->origin;
     const dim3 block(BX, BY);
     const size_t smem = sizeof(BwdSmem);
-    CK(cudaEventRecord(x->ev[2], x->st));
     long long launches = 0;
-    for (int m = x->nt_run; m >= 1; --m) {
-        const int nact = active_slots(x, m);
-        P.step = m;
-        P.pcur = x->F + (long long)((m - 1) & 1) * half + x->origin;   // p^{m-1}
-        P.pold = x->F + (long long)(m & 1) * half + x->origin;         // p^m -> p^{m-2}
-        P.bcur = x->A + (long long)((m + 1) & 1) * half + x->origin;   // b^{m+1}
-        P.bold = x->A + (long long)(m & 1) * half + x->origin;         // b^{m+2} -> b^m
-        P.psr = x->psiA + (long long)(m & 1) * phalf;
-        P.psw = x->psiA + (long long)((m + 1) & 1) * phalf;
-        k_backward<<<dim3(x->g.ntx, x->g.ntz, nact), block, smem, x->st>>>(P);
-        ++launches;
+    const int groups = x->cfg.plain_per_shot ? x->nshots : 1;
+    for (int grp = 0; grp < groups; ++grp) {
+        const int nt_grp = x->cfg.plain_per_shot ? x->nt_slot[grp] : x->nt_run;
+        for (int m = nt_grp; m >= 1; --m) {
+            const int nact = x->cfg.plain_per_shot ? 1 : active_slots(x, m);
+            P.shot_base = x->cfg.plain_per_shot ? grp : 0;
+            P.step = m;
+            P.pcur = x->F + (long long)((m - 1) & 1) * half + x->origin;   // p^{m-1}
+            P.pold = x->F + (long long)(m & 1) * half + x->origin;         // p^m -> p^{m-2}
+            P.bcur = x->A + (long long)((m + 1) & 1) * half + x->origin;   // b^{m+1}
+            P.bold = x->A + (long long)(m & 1) * half + x->origin;         // b^{m+2} -> b^m
+            P.psr = x->psiA + (long long)(m & 1) * phalf;
+            P.psw = x->psiA + (long long)((m + 1) & 1) * phalf;
+            k_backward<<<dim3(x->g.ntx, x->g.ntz, nact), block, smem, x->st>>>(P);
+            ++launches;
+        }
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(x->ev[3], x->st));
     // FP64 reduction over shots and the 2/v factor
     k_reduce<<<dim3((x->g.nx + 255) / 256, x->g.nz), 256, 0, x->st>>>(x->Gacc + x->origin, x->vel, x->grad, x->g, x->nshots);
     CK(cudaGetLastError());
@@ -258,6 +278,44 @@ float event_ms(cudaEvent_t a, cudaEvent_t b)
 int finish(fwi_ctx* x)
 {
     CK(cudaStreamSynchronize(x->st));
+    return FWI_OK;
+}
+
+enum Phase { PH_FWD = 0, PH_MIS = 1, PH_BWD = 2 };
+
+int run_phase_direct(fwi_ctx* x, int ph)
+{
+    return ph == PH_FWD ? run_forward(x) : ph == PH_MIS ? run_misfit(x) : run_backward(x);
+}
+
+// Runs one phase between its two timing events (forward ev0/ev1, misfit
+// ev4/ev5, backward ev2/ev3).  With use_graph the phase is captured once
+// into a CUDA graph and replayed; the events stay outside the graphs so that
+// their elapsed times are defined.
+int run_phase(fwi_ctx* x, int ph, bool graph)
+{
+    static const int evs[3][2] = {{0, 1}, {4, 5}, {2, 3}};
+    CK(cudaEventRecord(x->ev[evs[ph][0]], x->st));
+    if (!graph) {
+        int s = run_phase_direct(x, ph);
+        if (s) return s;
+    } else {
+        if (!x->gexec[ph]) {
+            const long long before = x->stats.launches;
+            CK(cudaStreamBeginCapture(x->st, cudaStreamCaptureModeThreadLocal));
+            int s = run_phase_direct(x, ph);
+            cudaGraph_t gr = nullptr;
+            cudaError_t e = cudaStreamEndCapture(x->st, &gr);
+            if (s) { if (gr) cudaGraphDestroy(gr); return s; }
+            if (e != cudaSuccess) return cuda_fail(x, e, "cudaStreamEndCapture");
+            x->graph[ph] = gr;
+            e = cudaGraphInstantiate(&x->gexec[ph], gr, 0);
+            if (e != cudaSuccess) { drop_graph(x); return cuda_fail(x, e, "cudaGraphInstantiate"); }
+            x->graph_launches[ph] = ph == PH_FWD ? x->stats.launches : x->stats.launches - before;
+        }
+        CK(cudaGraphLaunch(x->gexec[ph], x->st));
+    }
+    CK(cudaEventRecord(x->ev[evs[ph][1]], x->st));
     return FWI_OK;
 }
 
@@ -314,7 +372,9 @@ int fwi_check_config(const fwi_config* cfg)
     if (cfg->nt_max < 1 || cfg->jump < 1) return FWI_ERR_ARG;
     if (!(cfg->pml_max_f > 0) || !(cfg->pml_max_v > 0) || !(cfg->pml_coef_r > 0 && cfg->pml_coef_r < 1)) return FWI_ERR_ARG;
     if (cfg->free_surface != 0 && cfg->free_surface != 1) return FWI_ERR_ARG;
-    for (int i = 0; i < 7; ++i) if (cfg->reserved[i]) return FWI_ERR_ARG;
+    if ((cfg->use_graph != 0 && cfg->use_graph != 1) || (cfg->plain_per_shot != 0 && cfg->plain_per_shot != 1))
+        return FWI_ERR_ARG;
+    for (int i = 0; i < 6; ++i) if (cfg->reserved[i]) return FWI_ERR_ARG;
     return FWI_OK;
 }
 
@@ -341,7 +401,8 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
         return bail(FWI_ERR_NODEVICE);
     }
     if (cudaSetDevice(cfg->device) != cudaSuccess) return bail(FWI_ERR_NODEVICE);
-    if (cudaStreamCreateWithFlags(&x->st, cudaStreamNonBlocking) != cudaSuccess) return bail(FWI_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&x->own, cudaStreamNonBlocking) != cudaSuccess) return bail(FWI_ERR_CUDA);
+    x->st = x->own;
     for (auto& e : x->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return bail(FWI_ERR_CUDA);
 
@@ -407,7 +468,7 @@ void fwi_destroy(fwi_ctx* x)
     void* ps[] = {x->K, x->vel, x->pmlc, x->grad, x->gradf};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& e : x->ev) if (e) cudaEventDestroy(e);
-    if (x->st) cudaStreamDestroy(x->st);
+    if (x->own) cudaStreamDestroy(x->own);
     delete x;
 }
 
@@ -569,6 +630,7 @@ static void record_stats(fwi_ctx* x, bool fwd, bool mis, bool bwd)
     x->stats.ms_forward = fwd ? event_ms(x->ev[0], x->ev[1]) : 0.0;
     x->stats.ms_misfit = mis ? event_ms(x->ev[4], x->ev[5]) : 0.0;
     x->stats.ms_backward = bwd ? event_ms(x->ev[2], x->ev[3]) : 0.0;
+    x->stats.ms_total = event_ms(x->ev[6], x->ev[7]);
     x->stats.cell_steps = cs * ((fwd ? 1 : 0) + (bwd ? 2 : 0));
     x->stats.device_bytes = (long long)(x->bytes_model + x->bytes_shots);
 }
@@ -578,9 +640,11 @@ int fwi_forward(fwi_ctx* x, float* syn_out)
     if (!x) return FWI_ERR_ARG;
     if (!x->have_model || !x->nshots) return fail(x, FWI_ERR_STATE, "fwi_set_model and fwi_set_shots first");
     CK(cudaSetDevice(x->cfg.device));
-    int s = run_forward(x);
+    CK(cudaEventRecord(x->ev[6], x->st));
+    int s = run_phase(x, PH_FWD, false);
     if (s) return s;
     if (syn_out) CK(cudaMemcpyAsync(syn_out, x->syn, sizeof(float) * x->nsamples, cudaMemcpyDeviceToHost, x->st));
+    CK(cudaEventRecord(x->ev[7], x->st));
     s = finish(x);
     if (s) return s;
     record_stats(x, true, false, false);
@@ -593,11 +657,14 @@ int fwi_backward(fwi_ctx* x, const float* residual, double* grad_out)
     if (!x || !residual) return fail(x, FWI_ERR_ARG, "null argument");
     if (!x->have_fwd) return fail(x, FWI_ERR_STATE, "fwi_forward on the current model first");
     CK(cudaSetDevice(x->cfg.device));
+    CK(cudaEventRecord(x->ev[6], x->st));
     CK(cudaMemcpyAsync(x->res, residual, sizeof(float) * x->nsamples, cudaMemcpyHostToDevice, x->st));
-    int s = run_backward(x);
+    x->stats.launches = 0;
+    int s = run_phase(x, PH_BWD, false);
     if (s) return s;
     if (grad_out)
         CK(cudaMemcpyAsync(grad_out, x->grad, sizeof(double) * x->g.nx * x->g.nz, cudaMemcpyDeviceToHost, x->st));
+    CK(cudaEventRecord(x->ev[7], x->st));
     s = finish(x);
     x->have_fwd = false;   // the rebuild consumed the final forward fields
     if (s) return s;
@@ -612,12 +679,13 @@ static int gradient_impl(fwi_ctx* x, double* misfit)
         return fail(x, FWI_ERR_STATE, "fwi_set_model, fwi_set_shots and fwi_set_observed first");
     CK(cudaSetDevice(x->cfg.device));
     x->have_fwd = false;
-    int s = run_forward(x);
+    CK(cudaEventRecord(x->ev[6], x->st));
+    const bool graph = x->cfg.use_graph != 0;
+    int s = run_phase(x, PH_FWD, graph);
+    if (!s) s = run_phase(x, PH_MIS, graph);
+    if (!s) s = run_phase(x, PH_BWD, graph);
     if (s) return s;
-    s = run_misfit(x);
-    if (s) return s;
-    s = run_backward(x);
-    if (s) return s;
+    if (graph) x->stats.launches = x->graph_launches[0] + x->graph_launches[1] + x->graph_launches[2];
     if (misfit) CK(cudaMemcpyAsync(misfit, x->mis, 2 * sizeof(double), cudaMemcpyDeviceToHost, x->st));
     return FWI_OK;
 }
@@ -628,6 +696,7 @@ int fwi_gradient(fwi_ctx* x, double* misfit, double* grad_out)
     if (s) return s;
     if (grad_out)
         CK(cudaMemcpyAsync(grad_out, x->grad, sizeof(double) * x->g.nx * x->g.nz, cudaMemcpyDeviceToHost, x->st));
+    CK(cudaEventRecord(x->ev[7], x->st));
     s = finish(x);
     if (s) return s;
     record_stats(x, true, true, true);
@@ -644,6 +713,7 @@ int fwi_gradient_f32(fwi_ctx* x, double* misfit, float* grad_out)
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(grad_out, x->gradf, sizeof(float) * n, cudaMemcpyDeviceToHost, x->st));
     }
+    CK(cudaEventRecord(x->ev[7], x->st));
     s = finish(x);
     if (s) return s;
     record_stats(x, true, true, true);
@@ -651,6 +721,15 @@ int fwi_gradient_f32(fwi_ctx* x, double* misfit, float* grad_out)
 }
 
 const double* fwi_grad_device(const fwi_ctx* x) { return x ? x->grad : nullptr; }
+
+int fwi_set_stream(fwi_ctx* x, void* stream)
+{
+    if (!x) return FWI_ERR_ARG;
+    CK(cudaSetDevice(x->cfg.device));
+    CK(cudaStreamSynchronize(x->st));
+    x->st = stream ? (cudaStream_t)stream : x->own;
+    return FWI_OK;
+}
 
 int fwi_get_stats(const fwi_ctx* x, fwi_stats* out)
 {

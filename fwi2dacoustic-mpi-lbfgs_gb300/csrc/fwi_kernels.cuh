@@ -112,6 +112,7 @@ struct StepParams {
     int strip_len;
     int step;                // forward: it; backward: m
     int jump;
+    int shot_base;           // slot of blockIdx.z == 0 (non-zero only when shots run one by one)
 };
 
 __device__ __forceinline__ bool tile_general(const Geo& g, int x0, int z0)
@@ -351,7 +352,7 @@ __global__ void __launch_bounds__(NTH) k_forward(const StepParams P)
 {
     __shared__ __align__(16) float sp[SPH * SPW];
     __shared__ __align__(16) float su[TZ * UWP];
-    const int s = blockIdx.z;
+    const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = P.shots[s];
     if (P.step >= sd.nt) return;
     const Geo& g = P.g;
@@ -625,7 +626,7 @@ __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
-    const int s = blockIdx.z;
+    const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = P.shots[s];
     const int m = P.step;
     if (m > sd.nt) return;

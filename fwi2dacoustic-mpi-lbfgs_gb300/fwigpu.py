@@ -29,7 +29,8 @@ class FwiConfig(C.Structure):
     _fields_ = [("nx", C.c_int), ("nz", C.c_int), ("dx", C.c_float), ("dz", C.c_float), ("dt", C.c_float),
                 ("nt_max", C.c_int), ("npml", C.c_int), ("free_surface", C.c_int), ("jump", C.c_int),
                 ("pml_max_f", C.c_float), ("pml_max_v", C.c_float), ("pml_coef_r", C.c_float),
-                ("device", C.c_int), ("use_graph", C.c_int), ("reserved", C.c_int * 7)]
+                ("device", C.c_int), ("use_graph", C.c_int), ("plain_per_shot", C.c_int),
+                ("reserved", C.c_int * 6)]
 
 
 class FwiShot(C.Structure):
@@ -39,7 +40,7 @@ class FwiShot(C.Structure):
 
 class FwiStats(C.Structure):
     _fields_ = [("ms_forward", C.c_double), ("ms_backward", C.c_double), ("ms_misfit", C.c_double),
-                ("ms_reduce", C.c_double), ("cell_steps", C.c_double), ("launches", C.c_longlong),
+                ("ms_total", C.c_double), ("cell_steps", C.c_double), ("launches", C.c_longlong),
                 ("device_bytes", C.c_longlong)]
 
 
@@ -76,6 +77,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.fwi_grad_device.argtypes = [P]
     lib.fwi_grad_device.restype = P
     lib.fwi_get_stats.argtypes = [P, C.POINTER(FwiStats)]
+    lib.fwi_set_stream.argtypes = [P, P]
     lib.fwi_status_string.argtypes = [I]
     lib.fwi_status_string.restype = C.c_char_p
     lib.fwi_last_error.argtypes = [P]
@@ -97,13 +99,13 @@ def _dp(a):
 
 
 def make_config(nx, nz, dx, dz, dt, nt_max, npml=20, free_surface=1, jump=1, pml_max_f=15.0,
-                pml_max_v=6000.0, pml_coef_r=0.001, device=0, use_graph=0) -> FwiConfig:
+                pml_max_v=6000.0, pml_coef_r=0.001, device=0, use_graph=0, plain_per_shot=0) -> FwiConfig:
     """CPML defaults are MAX_F, MAX_V, COEF_R of fwi_sys.h:2-4."""
     cfg = FwiConfig()
     cfg.nx, cfg.nz, cfg.dx, cfg.dz, cfg.dt = nx, nz, dx, dz, dt
     cfg.nt_max, cfg.npml, cfg.free_surface, cfg.jump = nt_max, npml, int(free_surface), jump
     cfg.pml_max_f, cfg.pml_max_v, cfg.pml_coef_r = pml_max_f, pml_max_v, pml_coef_r
-    cfg.device, cfg.use_graph = device, use_graph
+    cfg.device, cfg.use_graph, cfg.plain_per_shot = device, use_graph, plain_per_shot
     return cfg
 
 
@@ -195,17 +197,31 @@ class Engine:
         self._check(self.lib.fwi_backward(self.ctx, _fp(res), _dp(grad)), "fwi_backward")
         return grad
 
-    def gradient(self, keep_on_device=False):
+    def gradient(self, keep_on_device=False, out=None):
+        """Misfit and dJ/dv.  ``out`` (float64 [nz][nx], e.g. pinned memory)
+        receives the gradient; ``keep_on_device`` leaves it on the device."""
         mis = np.zeros(2, np.float64)
-        grad = None if keep_on_device else np.zeros((self.cfg.nz, self.cfg.nx), np.float64)
+        grad = None
+        if not keep_on_device:
+            grad = out if out is not None else np.zeros((self.cfg.nz, self.cfg.nx), np.float64)
+            assert grad.dtype == np.float64 and grad.size == self.cfg.nz * self.cfg.nx and grad.flags.c_contiguous
         self._check(self.lib.fwi_gradient(self.ctx, _dp(mis), _dp(grad)), "fwi_gradient")
         return float(mis[1]), grad
+
+    def grad_device_ptr(self) -> int:
+        return int(self.lib.fwi_grad_device(self.ctx) or 0)
 
     def gradient_f32(self):
         mis = np.zeros(2, np.float64)
         grad = np.zeros((self.cfg.nz, self.cfg.nx), np.float32)
         self._check(self.lib.fwi_gradient_f32(self.ctx, _dp(mis), _fp(grad)), "fwi_gradient_f32")
         return float(mis[1]), grad
+
+    def set_stream(self, stream_ptr):
+        """Run on the caller's cudaStream_t (an int handle, e.g. torch's
+        ``torch.cuda.current_stream().cuda_stream``); None restores the own stream."""
+        self._check(self.lib.fwi_set_stream(self.ctx, C.c_void_p(stream_ptr) if stream_ptr else None),
+                    "fwi_set_stream")
 
     def stats(self) -> dict:
         s = FwiStats()

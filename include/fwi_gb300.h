@@ -61,8 +61,11 @@ typedef struct fwi_config {
     float pml_max_v;       /* MAX_V  (fwi_sys.h:3), e.g. 6000 */
     float pml_coef_r;      /* COEF_R (fwi_sys.h:4), e.g. 0.001 */
     int   device;          /* CUDA device ordinal */
-    int   use_graph;       /* 1: replay the time loops as one CUDA graph */
-    int   reserved[7];     /* must be zero */
+    int   use_graph;       /* 1: capture the whole gradient (both time loops)
+                              once and replay it as one CUDA graph */
+    int   plain_per_shot;  /* 1: run shots one after another, one shot per
+                              launch (the unbatched path, for comparison) */
+    int   reserved[6];     /* must be zero */
 } fwi_config;
 
 /* One shot.  Positions are metres, converted to cells as fwi_init does:
@@ -79,7 +82,7 @@ typedef struct fwi_stats {
     double ms_forward;     /* device time of the last forward loop */
     double ms_backward;    /* device time of the last backward loop */
     double ms_misfit;      /* device time of the misfit/residual kernel */
-    double ms_reduce;      /* device time of the FP64 shot reduction */
+    double ms_total;       /* device time of the last public call, stream order */
     double cell_steps;     /* physical cell-steps of the last gradient (x3 for fwd+rebuild+adjoint) */
     long long launches;    /* kernels launched by the last gradient */
     long long device_bytes;/* device memory held by the context */
@@ -128,6 +131,11 @@ int fwi_gradient_f32(fwi_ctx *ctx, double *misfit, float *grad_out);
 
 /* Device pointer of the FP64 gradient [nz][nx] of the last backward pass. */
 const double *fwi_grad_device(const fwi_ctx *ctx);
+
+/* Orders all later work of the context on the caller's CUDA stream
+ * (a cudaStream_t of the context's device; NULL restores the context's own
+ * stream).  Calls still complete before they return. */
+int fwi_set_stream(fwi_ctx *ctx, void *stream);
 
 int fwi_get_stats(const fwi_ctx *ctx, fwi_stats *out);
 const char *fwi_status_string(int status);
