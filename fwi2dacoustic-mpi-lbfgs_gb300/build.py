@@ -42,6 +42,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     tmp = LIB + ".tmp"
     cmd = [nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
            "-I", os.path.join(ROOT, "include"), "-o", tmp] + SOURCES
+    # FWI_NVCC_EXTRA adds diagnostics flags, e.g. -DFWI_ALIGN_CHECK
+    cmd[1:1] = os.environ.get("FWI_NVCC_EXTRA", "").split()
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -53,5 +55,30 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+EMU_LIB = os.path.join(PKG, "libfwiemu.so")
+
+
+def build_emu(force: bool = False, sanitize: bool = True) -> str:
+    """CPU emulation build of the same sources (csrc/cpu_emu.h) for memory-
+    safety checks without a GPU: every kernel runs on host threads, every
+    device buffer is an exact-size heap block, AddressSanitizer on."""
+    if not force and os.path.isfile(EMU_LIB) and all(os.path.getmtime(d) <= os.path.getmtime(EMU_LIB)
+                                                     for d in DEPS + [os.path.join(PKG, "csrc", "cpu_emu.h")]):
+        return EMU_LIB
+    cxx = os.environ.get("CXX", "g++")
+    cmd = [cxx, "-x", "c++", "-std=c++20", "-O1", "-g", "-fPIC", "-shared", "-DFWI_CPU_EMU",
+           "-Wno-unknown-pragmas", "-I", os.path.join(ROOT, "include"), "-o", EMU_LIB + ".tmp"] + SOURCES + ["-lpthread"]
+    if sanitize:
+        cmd[1:1] = ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("emulation build failed:\n" + r.stdout + r.stderr)
+    os.replace(EMU_LIB + ".tmp", EMU_LIB)
+    return EMU_LIB
+
+
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    if "--emu" in sys.argv:
+        print(build_emu(force="--force" in sys.argv))
+    else:
+        print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

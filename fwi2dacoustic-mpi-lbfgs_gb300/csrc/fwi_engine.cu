@@ -98,8 +98,13 @@ struct fwi_ctx {
     double* partial = nullptr;
     double* mis = nullptr;
     ShotDev* shots_d = nullptr;
-    RecDev* recs_d = nullptr;
-    int* rtile_d = nullptr;
+    RecSample* samp_d = nullptr;   // receivers, slot order (forward sampling)
+    RecDev* recs_d = nullptr;      // receivers grouped by tile (backward injection)
+    int* rtile_d = nullptr;        // per-slot, per-tile CSR of recs_d
+    int2* gen_d = nullptr;         // tiles of the general path
+    int ngen = 0;
+    int ftx0 = 0, ftx1 = 0, ftz0 = 0, ftz1 = 0;   // interior tile rectangle
+    std::vector<int> samp_off;                    // per-slot ranges (nshots + 1)
     std::vector<int> nt_slot;      // nt of each slot, descending
     long long nsamples = 0;
     int npartial = 0;
@@ -156,10 +161,12 @@ void free_shots(fwi_ctx* x)
 {
     drop_graph(x);
     void* ps[] = {x->F, x->A, x->Gacc, x->psiF, x->psiA, x->ring, x->syn, x->res, x->obs, x->wav,
-                  x->shots_d, x->recs_d, x->rtile_d, x->partial, x->mis};
+                  x->shots_d, x->samp_d, x->recs_d, x->rtile_d, x->partial, x->mis};
     for (void* p : ps) if (p) cudaFree(p);
     x->F = x->A = x->Gacc = x->psiF = x->psiA = x->ring = x->syn = x->res = x->obs = x->wav = nullptr;
-    x->shots_d = nullptr; x->recs_d = nullptr; x->rtile_d = nullptr; x->partial = nullptr; x->mis = nullptr;
+    x->shots_d = nullptr; x->samp_d = nullptr; x->recs_d = nullptr; x->rtile_d = nullptr;
+    x->partial = nullptr; x->mis = nullptr;
+    x->samp_off.clear();
     x->nshots = 0; x->nt_run = 0; x->nsamples = 0; x->bytes_shots = 0;
     x->nt_slot.clear();
     x->have_obs = x->have_fwd = false;
@@ -174,6 +181,9 @@ StepParams base_params(const fwi_ctx* x)
     P.pmlc = x->pmlc;
     P.pl = x->pl;
     P.shots = x->shots_d;
+    P.gen_tiles = x->gen_d;
+    P.fast_tx0 = x->ftx0;
+    P.fast_tz0 = x->ftz0;
     P.recs = x->recs_d;
     P.rtile = x->rtile_d;
     P.wav = x->wav;
@@ -192,6 +202,70 @@ int active_slots(const fwi_ctx* x, int pred_ge)   // shots with nt >= pred_ge
     return n;
 }
 
+// FWI_ALIGN_CHECK builds synchronise after every launch and name the kernel
+// that failed (diagnostics only).
+#ifdef FWI_ALIGN_CHECK
+#define DIAG_SYNC(tag)                                                                        \
+    do {                                                                                      \
+        cudaError_t e_ = cudaStreamSynchronize(x->st);                                       \
+        if (e_ != cudaSuccess) { fprintf(stderr, "FWI diag: %s failed: %s\n", tag, cudaGetErrorString(e_)); } \
+    } while (0)
+#else
+#define DIAG_SYNC(tag) do {} while (0)
+#endif
+
+RecParams rec_params(const fwi_ctx* x, float* field, int step)
+{
+    RecParams Q{};
+    Q.g = x->g;
+    Q.shots = x->shots_d;
+    Q.recs = x->samp_d;
+    Q.field = field;
+    Q.syn = x->syn;
+    Q.step = step;
+    Q.jump = x->cfg.jump;
+    return Q;
+}
+
+// One forward step of the shots [lo, hi): interior tiles, general tiles,
+// then receiver sampling.
+long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
+{
+    const dim3 block(BX, BY);
+    const int n = hi - lo;
+    long long l = 0;
+    P.shot_base = lo;
+    if (x->ftx1 > x->ftx0 && x->ftz1 > x->ftz0) {
+        FWI_LAUNCH(k_fwd_fast, dim3(x->ftx1 - x->ftx0, x->ftz1 - x->ftz0, n), block, 0, x->st, P);
+        DIAG_SYNC("k_fwd_fast");
+        ++l;
+    }
+    if (x->ngen) {
+        FWI_LAUNCH(k_fwd_gen, dim3(x->ngen, 1, n), block, 0, x->st, P);
+        DIAG_SYNC("k_fwd_gen");
+        ++l;
+    }
+    if (P.step % x->cfg.jump == 0) {
+        RecParams Q = rec_params(x, P.pold, P.step);
+        Q.lo = x->samp_off[lo];
+        Q.hi = x->samp_off[hi];
+        if (Q.hi > Q.lo) {
+            FWI_LAUNCH(k_sample, (Q.hi - Q.lo + 255) / 256, 256, 0, x->st, Q);
+            DIAG_SYNC("k_sample");
+            ++l;
+        }
+    }
+    return l;
+}
+
+long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
+{
+    P.shot_base = lo;
+    FWI_LAUNCH(k_backward, dim3(x->g.ntx, x->g.ntz, hi - lo), dim3(BX, BY), sizeof(BwdSmem), x->st, P);
+    DIAG_SYNC("k_backward");
+    return 1;
+}
+
 int run_forward(fwi_ctx* x)
 {
     const long long half = (long long)x->nshots * x->g.fstride;
@@ -199,22 +273,20 @@ int run_forward(fwi_ctx* x)
     CK(cudaMemsetAsync(x->F, 0, sizeof(float) * 2 * half, x->st));
     CK(cudaMemsetAsync(x->psiF, 0, sizeof(float) * 2 * phalf, x->st));
     StepParams P = base_params(x);
-    const dim3 block(BX, BY);
     long long launches = 0;
     // batched: one launch per step over the active shots; plain: shot after shot
     const int groups = x->cfg.plain_per_shot ? x->nshots : 1;
     for (int grp = 0; grp < groups; ++grp) {
         const int nt_grp = x->cfg.plain_per_shot ? x->nt_slot[grp] : x->nt_run;
         for (int it = 0; it < nt_grp; ++it) {
-            const int nact = x->cfg.plain_per_shot ? 1 : active_slots(x, it + 1);
-            P.shot_base = x->cfg.plain_per_shot ? grp : 0;
+            const int lo = x->cfg.plain_per_shot ? grp : 0;
+            const int hi = x->cfg.plain_per_shot ? grp + 1 : active_slots(x, it + 1);
             P.step = it;
             P.pcur = x->F + (long long)(it & 1) * half + x->origin;
             P.pold = x->F + (long long)((it + 1) & 1) * half + x->origin;
             P.psr = x->psiF + (long long)(it & 1) * phalf;
             P.psw = x->psiF + (long long)((it + 1) & 1) * phalf;
-            k_forward<<<dim3(x->g.ntx, x->g.ntz, nact), block, 0, x->st>>>(P);
-            ++launches;
+            launches += launch_fwd_step(x, P, lo, hi);
         }
     }
     CK(cudaGetLastError());
@@ -224,8 +296,10 @@ int run_forward(fwi_ctx* x)
 
 int run_misfit(fwi_ctx* x)
 {
-    k_misfit<<<x->npartial, 256, 0, x->st>>>(x->syn, x->obs, x->res, x->nsamples, x->partial);
-    k_misfit_final<<<1, 256, 0, x->st>>>(x->partial, x->npartial, x->mis);
+    FWI_LAUNCH(k_misfit, x->npartial, 256, 0, x->st, x->syn, x->obs, x->res, x->nsamples, x->partial);
+    DIAG_SYNC("k_misfit");
+    FWI_LAUNCH(k_misfit_final, 1, 256, 0, x->st, x->partial, x->npartial, x->mis);
+    DIAG_SYNC("k_misfit_final");
     CK(cudaGetLastError());
     x->stats.launches += 2;
     return FWI_OK;
@@ -240,15 +314,13 @@ int run_backward(fwi_ctx* x)
     CK(cudaMemsetAsync(x->Gacc, 0, sizeof(float) * half, x->st));
     StepParams P = base_params(x);
     P.gacc = x->Gacc + x->origin;
-    const dim3 block(BX, BY);
-    const size_t smem = sizeof(BwdSmem);
     long long launches = 0;
     const int groups = x->cfg.plain_per_shot ? x->nshots : 1;
     for (int grp = 0; grp < groups; ++grp) {
         const int nt_grp = x->cfg.plain_per_shot ? x->nt_slot[grp] : x->nt_run;
         for (int m = nt_grp; m >= 1; --m) {
-            const int nact = x->cfg.plain_per_shot ? 1 : active_slots(x, m);
-            P.shot_base = x->cfg.plain_per_shot ? grp : 0;
+            const int lo = x->cfg.plain_per_shot ? grp : 0;
+            const int hi = x->cfg.plain_per_shot ? grp + 1 : active_slots(x, m);
             P.step = m;
             P.pcur = x->F + (long long)((m - 1) & 1) * half + x->origin;   // p^{m-1}
             P.pold = x->F + (long long)(m & 1) * half + x->origin;         // p^m -> p^{m-2}
@@ -256,13 +328,12 @@ int run_backward(fwi_ctx* x)
             P.bold = x->A + (long long)(m & 1) * half + x->origin;         // b^{m+2} -> b^m
             P.psr = x->psiA + (long long)(m & 1) * phalf;
             P.psw = x->psiA + (long long)((m + 1) & 1) * phalf;
-            k_backward<<<dim3(x->g.ntx, x->g.ntz, nact), block, smem, x->st>>>(P);
-            ++launches;
+            launches += launch_bwd_step(x, P, lo, hi);
         }
     }
     CK(cudaGetLastError());
     // FP64 reduction over shots and the 2/v factor
-    k_reduce<<<dim3((x->g.nx + 255) / 256, x->g.nz), 256, 0, x->st>>>(x->Gacc + x->origin, x->vel, x->grad, x->g, x->nshots);
+    FWI_LAUNCH(k_reduce, dim3((x->g.nx + 255) / 256, x->g.nz), 256, 0, x->st, x->Gacc + x->origin, x->vel, x->grad, x->g, x->nshots);
     CK(cudaGetLastError());
     x->stats.launches += launches + 1;
     return FWI_OK;
@@ -418,6 +489,25 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     g.fstride = (long long)x->rows_alloc * g.ld;
     x->origin = (long long)MZ * g.ld + MX;
 
+    // interior tile rectangle and the list of general-path tiles
+    {
+        std::vector<int2> gen;
+        int tx0 = -1, tx1 = -1, tz0 = -1, tz1 = -1;
+        for (int t = 0; t < g.ntx; ++t)
+            if (!tile_x_general(g, t * TX)) { if (tx0 < 0) tx0 = t; tx1 = t + 1; }
+        for (int t = 0; t < g.ntz; ++t)
+            if (!tile_z_general(g, t * TZ)) { if (tz0 < 0) tz0 = t; tz1 = t + 1; }
+        if (tx0 < 0 || tz0 < 0) tx0 = tx1 = tz0 = tz1 = 0;
+        for (int tz = 0; tz < g.ntz; ++tz)
+            for (int tx = 0; tx < g.ntx; ++tx)
+                if (!(tx >= tx0 && tx < tx1 && tz >= tz0 && tz < tz1)) gen.push_back(make_int2(tx, tz));
+        x->ftx0 = tx0; x->ftx1 = tx1; x->ftz0 = tz0; x->ftz1 = tz1;
+        x->ngen = (int)gen.size();
+        if (dalloc(x, &x->gen_d, gen.size(), &x->bytes_model)) return bail(FWI_ERR_NOMEM);
+        if (!gen.empty() && cudaMemcpy(x->gen_d, gen.data(), gen.size() * sizeof(int2), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(FWI_ERR_CUDA);
+    }
+
     float fd[8];
     fd_coefficients(cfg->dx, cfg->dz, fd);
     Coef& c = x->c;
@@ -454,7 +544,11 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     if (dalloc(x, &x->grad, (size_t)g.nx * g.nz, &x->bytes_model)) return bail(FWI_ERR_NOMEM);
     if (dalloc(x, &x->gradf, (size_t)g.nx * g.nz, &x->bytes_model)) return bail(FWI_ERR_NOMEM);
     if (cudaMemcpy(x->pmlc, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return bail(FWI_ERR_CUDA);
-    if (cudaMemset(x->K, 0, sizeof(float) * g.fstride) != cudaSuccess) return bail(FWI_ERR_CUDA);
+    // on the context's stream: a legacy-stream memset would not be ordered
+    // before k_build_K, which runs on the non-blocking stream
+    if (cudaMemsetAsync(x->K, 0, sizeof(float) * g.fstride, x->st) != cudaSuccess ||
+        cudaStreamSynchronize(x->st) != cudaSuccess)
+        return bail(FWI_ERR_CUDA);
     if (cudaFuncSetAttribute(k_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BwdSmem)) != cudaSuccess)
         return bail(FWI_ERR_CUDA);
     if (status) *status = FWI_OK;
@@ -465,7 +559,7 @@ void fwi_destroy(fwi_ctx* x)
 {
     if (!x) return;
     free_shots(x);
-    void* ps[] = {x->K, x->vel, x->pmlc, x->grad, x->gradf};
+    void* ps[] = {x->K, x->vel, x->pmlc, x->grad, x->gradf, x->gen_d};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& e : x->ev) if (e) cudaEventDestroy(e);
     if (x->own) cudaStreamDestroy(x->own);
@@ -490,7 +584,7 @@ int fwi_set_model(fwi_ctx* x, const float* vel)
     if (cfl > 1.0) return fail(x, FWI_ERR_CFL, "CFL number " + std::to_string(cfl) + " > 1");
     CK(cudaSetDevice(x->cfg.device));
     CK(cudaMemcpyAsync(x->vel, vel, n * sizeof(float), cudaMemcpyHostToDevice, x->st));
-    k_build_K<<<dim3((g.pnx + 255) / 256, g.pnz), 256, 0, x->st>>>(x->vel, x->K + x->origin, g, x->cfg.dt);
+    FWI_LAUNCH(k_build_K, dim3((g.pnx + 255) / 256, g.pnz), 256, 0, x->st, x->vel, x->K + x->origin, g, x->cfg.dt);
     CK(cudaGetLastError());
     int s = finish(x);
     if (s) return s;
@@ -507,8 +601,8 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     const int jump = x->cfg.jump;
     // validate and convert geometry (fwi_2d.c:357-371)
     std::vector<ShotDev> sd(nshots);
-    std::vector<std::vector<RecDev>> recs(nshots);
-    std::vector<std::vector<int>> rtiles(nshots);
+    struct Rec { long long foff, syn_base; };
+    std::vector<std::vector<Rec>> recs(nshots);
     long long syn_off = 0, wav_tot = 0;
     std::vector<long long> wav_off(nshots);
     for (int s = 0; s < nshots; ++s) {
@@ -530,25 +624,14 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
         wav_off[s] = wav_tot;
         d.wav_off = (int)wav_tot;
         wav_tot += sh.nt;
-        std::vector<std::pair<int, RecDev>> tmp(sh.nr);
+        recs[s].resize(sh.nr);
         for (int r = 0; r < sh.nr; ++r) {
             int rx, rz;
             cell_of(sh.rec_xz[2 * r], sh.rec_xz[2 * r + 1], x->cfg.dx, x->cfg.dz, &rx, &rz);
             if (rx < 0 || rx >= g.nx || rz < 0 || rz >= g.nz)
                 return fail(x, FWI_ERR_GEOMETRY, "shot " + std::to_string(s) + ": receiver " + std::to_string(r) + " outside the model");
-            const int row = rz + g.z0p, col = rx + g.x0p;
-            const int tile = (row / TZ) * g.ntx + col / TX;
-            RecDev rd{};
-            rd.cell = (row % TZ) * TX + (col % TX);
-            rd.syn_base = syn_off + (long long)r * d.nt0;
-            tmp[r] = {tile, rd};
+            recs[s][r] = {(long long)(rz + g.z0p) * g.ld + rx + g.x0p, syn_off + (long long)r * d.nt0};
         }
-        std::stable_sort(tmp.begin(), tmp.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
-        const int ntiles = g.ntx * g.ntz;
-        rtiles[s].assign(ntiles + 1, 0);
-        for (auto& t : tmp) rtiles[s][t.first + 1]++;
-        for (int t = 0; t < ntiles; ++t) rtiles[s][t + 1] += rtiles[s][t];
-        for (auto& t : tmp) recs[s].push_back(t.second);
         syn_off += (long long)sh.nr * d.nt0;
     }
     // slots: shots sorted by nt, longest first, so the active shots of a step form a prefix
@@ -557,23 +640,44 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sd[a].nt > sd[b].nt; });
 
     free_shots(x);
-    const int ntiles = g.ntx * g.ntz;
     const long long strip_len = 2LL * NSTRIP * (g.nx + g.nz);
     std::vector<ShotDev> slot(nshots);
+    std::vector<RecSample> samp;
     std::vector<RecDev> rec_all;
     std::vector<int> rt_all;
     std::vector<float> wav_all(wav_tot);
     long long ring_off = 0;
+    const int ntiles = g.ntx * g.ntz;
     x->nt_slot.resize(nshots);
+    x->samp_off.assign(nshots + 1, 0);
     for (int k = 0; k < nshots; ++k) {
         const int s = order[k];
         ShotDev d = sd[s];
         d.ring_off = ring_off;
         ring_off += (long long)d.nt * strip_len;
+        // sampling: one entry per receiver; injection: receivers grouped by
+        // tile (CSR), summed inside the tile in receiver order
+        std::vector<std::pair<int, RecDev>> tmp;
+        for (size_t r = 0; r < recs[s].size(); ++r) {
+            const long long foff = recs[s][r].foff;
+            samp.push_back(RecSample{k, 0, foff, recs[s][r].syn_base, 0});
+            const int row = (int)(foff / g.ld), col = (int)(foff % g.ld);
+            RecDev rd{};
+            rd.cell = (row % TZ) * TX + (col % TX);
+            rd.syn_base = recs[s][r].syn_base;
+            tmp.push_back({(row / TZ) * g.ntx + col / TX, rd});
+        }
+        std::stable_sort(tmp.begin(), tmp.end(), [](const auto& a, const auto& b2) { return a.first < b2.first; });
         d.rtile_off = (int)rt_all.size();
-        const int rbase = (int)rec_all.size();
-        for (int t = 0; t <= ntiles; ++t) rt_all.push_back(rtiles[s][t] + rbase);
-        rec_all.insert(rec_all.end(), recs[s].begin(), recs[s].end());
+        {
+            std::vector<int> cnt(ntiles + 1, 0);
+            for (auto& t : tmp) cnt[t.first + 1]++;
+            for (int t = 0; t < ntiles; ++t) cnt[t + 1] += cnt[t];
+            const int rbase = (int)rec_all.size();
+            for (int t = 0; t <= ntiles; ++t) rt_all.push_back(cnt[t] + rbase);
+            for (auto& t : tmp) rec_all.push_back(t.second);
+        }
+        x->samp_off[k + 1] = (int)samp.size();
         std::memcpy(&wav_all[wav_off[s]], shots[s].wavelet, sizeof(float) * shots[s].nt);
         slot[k] = d;
         x->nt_slot[k] = d.nt;
@@ -596,17 +700,38 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     e = e ? e : dalloc(x, &x->obs, (size_t)syn_off, &b);
     e = e ? e : dalloc(x, &x->wav, (size_t)wav_tot, &b);
     e = e ? e : dalloc(x, &x->shots_d, (size_t)nshots, &b);
+    e = e ? e : dalloc(x, &x->samp_d, samp.size(), &b);
     e = e ? e : dalloc(x, &x->recs_d, rec_all.size(), &b);
     e = e ? e : dalloc(x, &x->rtile_d, rt_all.size(), &b);
     e = e ? e : dalloc(x, &x->partial, (size_t)x->npartial, &b);
     e = e ? e : dalloc(x, &x->mis, 2, &b);
     if (e) { std::string m = x->err; free_shots(x); x->err = m; return e; }
     CK(cudaMemcpyAsync(x->shots_d, slot.data(), sizeof(ShotDev) * nshots, cudaMemcpyHostToDevice, x->st));
-    if (!rec_all.empty())
+    if (!samp.empty()) {
+        CK(cudaMemcpyAsync(x->samp_d, samp.data(), sizeof(RecSample) * samp.size(), cudaMemcpyHostToDevice, x->st));
         CK(cudaMemcpyAsync(x->recs_d, rec_all.data(), sizeof(RecDev) * rec_all.size(), cudaMemcpyHostToDevice, x->st));
+    }
     CK(cudaMemcpyAsync(x->rtile_d, rt_all.data(), sizeof(int) * rt_all.size(), cudaMemcpyHostToDevice, x->st));
     CK(cudaMemcpyAsync(x->wav, wav_all.data(), sizeof(float) * wav_all.size(), cudaMemcpyHostToDevice, x->st));
     CK(cudaMemsetAsync(x->syn, 0, sizeof(float) * std::max<long long>(1, syn_off), x->st));
+#ifdef FWI_ALIGN_CHECK
+    {
+        DbgRanges r{};
+        auto add = [&](const void* p, size_t bytes) {
+            if (p && r.n < 24) { r.lo[r.n] = (unsigned long long)p; r.hi[r.n] = (unsigned long long)p + bytes; ++r.n; }
+        };
+        add(x->F, sizeof(float) * 2 * half); add(x->A, sizeof(float) * 2 * half); add(x->Gacc, sizeof(float) * half);
+        add(x->psiF, sizeof(float) * 2 * phalf); add(x->psiA, sizeof(float) * 2 * phalf);
+        add(x->ring, sizeof(float) * ring_off); add(x->syn, sizeof(float) * syn_off); add(x->res, sizeof(float) * syn_off);
+        add(x->obs, sizeof(float) * syn_off); add(x->wav, sizeof(float) * wav_tot);
+        add(x->shots_d, sizeof(ShotDev) * nshots); add(x->samp_d, sizeof(RecSample) * samp.size());
+        add(x->recs_d, sizeof(RecDev) * rec_all.size()); add(x->rtile_d, sizeof(int) * rt_all.size());
+        add(x->K, sizeof(float) * g.fstride); add(x->vel, sizeof(float) * g.nx * g.nz); add(x->gen_d, sizeof(int2) * x->ngen);
+        add(x->pmlc, sizeof(float) * 8 * (2 * g.npml + 1));
+        CK(cudaMemcpyToSymbol(g_dbg, &r, sizeof(r)));
+        fprintf(stderr, "FWI diag: %d ranges\n", r.n);
+    }
+#endif
     return finish(x);
 }
 
@@ -709,7 +834,7 @@ int fwi_gradient_f32(fwi_ctx* x, double* misfit, float* grad_out)
     if (s) return s;
     const long long n = (long long)x->g.nx * x->g.nz;
     if (grad_out) {
-        k_to_float<<<256, 256, 0, x->st>>>(x->grad, x->gradf, n);
+        FWI_LAUNCH(k_to_float, 256, 256, 0, x->st, x->grad, x->gradf, n);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(grad_out, x->gradf, sizeof(float) * n, cudaMemcpyDeviceToHost, x->st));
     }

@@ -27,10 +27,53 @@
 //     fwi_2d.c:919-960),
 //   * the imaging condition g += b^m (L p^{m-1} + f^{m-1}).
 #pragma once
+#ifdef FWI_CPU_EMU
+#include "cpu_emu.h"
+#else
 #include <cuda_runtime.h>
+#include "cpu_emu.h"
+#endif
 #include <stdint.h>
+#include <cstdio>
 
 namespace fwi {
+
+// FWI_ALIGN_CHECK builds (diagnostics only) verify the alignment of every
+// vector or asynchronous access, report the offending address and skip it.
+#ifdef FWI_ALIGN_CHECK
+#define FWI_ALIGNED(ptr, n, tag)                                                                   \
+    ((((unsigned long long)(ptr)) % (n)) == 0 ||                                                   \
+     (printf("FWI misaligned %s: %p (mod %d = %llu) blk %d,%d,%d thr %d,%d\n", tag, (void*)(ptr), \
+             (int)(n), ((unsigned long long)(ptr)) % (n), blockIdx.x, blockIdx.y, blockIdx.z,     \
+             threadIdx.x, threadIdx.y), false))
+#else
+#define FWI_ALIGNED(ptr, n, tag) true
+#endif
+
+// Allocation table for FWI_ALIGN_CHECK builds: every checked access must fall
+// inside one of these [lo, hi) byte ranges and be aligned to its size.
+struct DbgRanges {
+    unsigned long long lo[24], hi[24];
+    int n;
+};
+#ifdef FWI_ALIGN_CHECK
+__device__ DbgRanges g_dbg;
+__device__ inline bool dbg_ok(const void* p, int bytes, const char* tag)
+{
+    const unsigned long long a = (unsigned long long)p;
+    bool in = false;
+    for (int i = 0; i < g_dbg.n; ++i)
+        if (a >= g_dbg.lo[i] && a + bytes <= g_dbg.hi[i]) { in = true; break; }
+    const bool al = (a % (unsigned long long)(bytes > 16 ? 16 : bytes)) == 0;
+    if (!in || !al)
+        printf("FWI bad access %s: %p (%d B) in=%d aligned=%d blk %d,%d,%d thr %d,%d\n", tag, p, bytes, (int)in,
+               (int)al, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y);
+    return in && al;
+}
+#define DBG_OK(p, bytes, tag) dbg_ok((p), (bytes), (tag))
+#else
+#define DBG_OK(p, bytes, tag) true
+#endif
 
 constexpr int TX = 64;             // tile width  (cells)
 constexpr int TZ = 32;             // tile height (cells)
@@ -73,7 +116,9 @@ struct PsiLayout {
     int u0, u1, v0, v1, ux0, ux1, vz0, vz1;
 };
 
-struct ShotDev {
+// Device-side records are padded to multiples of 16 bytes and 16-byte
+// aligned, so that every array element can be read with vector loads.
+struct alignas(16) ShotDev {
     int nt, nt0, nr;
     int src_r, src_c;        // source cell, padded coordinates
     int wav_off;             // offset of the wavelet in the wavelet pool
@@ -83,10 +128,29 @@ struct ShotDev {
     long long ring_off;      // offset of the shot's strip ring
 };
 
-struct RecDev {
+// One receiver, for sampling syn[r][k] = p^{k*jump+1}(receiver).
+struct alignas(16) RecSample {
+    int slot, pad0;
+    long long foff;          // row * ld + col of the receiver cell
+    long long syn_base;      // syn_off + r * nt0
+    long long pad1;
+};
+
+// One receiver for the backward injection, grouped by tile.
+struct alignas(16) RecDev {
     int cell;                // (row % TZ) * TX + (col % TX) inside its tile
     int pad;
     long long syn_base;      // syn_off + r * nt0
+};
+
+struct RecParams {
+    Geo g;
+    const ShotDev* shots;
+    const RecSample* recs;   // sampling
+    float* field;            // p^{it+1}
+    float* syn;
+    int lo, hi;              // receiver range of this launch
+    int step, jump;
 };
 
 struct StepParams {
@@ -103,8 +167,10 @@ struct StepParams {
     const float* pmlc;       // a0x b0x a1x b1x a0z b0z a1z b1z, 2*npml+1 each
     PsiLayout pl;
     const ShotDev* shots;
-    const RecDev* recs;
-    const int* rtile;
+    const int2* gen_tiles;   // tiles of the general path (x tile, z tile)
+    int fast_tx0, fast_tz0;  // first interior tile of the branch-free path
+    const RecDev* recs;      // backward: receivers grouped by tile
+    const int* rtile;        // backward: per-tile CSR of recs
     const float* wav;
     float* syn;              // forward: sampled traces
     const float* res;        // backward: adjoint sources
@@ -115,15 +181,19 @@ struct StepParams {
     int shot_base;           // slot of blockIdx.z == 0 (non-zero only when shots run one by one)
 };
 
-__device__ __forceinline__ bool tile_general(const Geo& g, int x0, int z0)
+// A tile takes the general path when its cells or their stencil halo touch a
+// grid edge (edge and one-sided formulas), a CPML layer (psi recursions) or
+// the boundary strips.  The test separates into x and z, so the interior
+// tiles form a rectangle.
+__host__ __device__ inline bool tile_x_general(const Geo& g, int x0)
 {
     const int np = g.npml;
-    if (x0 < 8 || x0 + TX + 8 > g.pnx) return true;               // x edges
-    if (x0 - 4 <= np || x0 + TX + 4 >= g.pnx - np) return true;   // x CPML
-    if (z0 < 8 || z0 + TZ + 8 > g.pnz) return true;               // z edges
-    if (z0 + TZ + 4 >= g.pnz - np) return true;                   // bottom CPML
-    if (!g.fs && z0 - 4 <= np) return true;                       // top CPML
-    return false;
+    return x0 < 8 || x0 + TX + 8 > g.pnx || x0 - 4 <= np || x0 + TX + 4 >= g.pnx - np;
+}
+__host__ __device__ inline bool tile_z_general(const Geo& g, int z0)
+{
+    const int np = g.npml;
+    return z0 < 8 || z0 + TZ + 8 > g.pnz || z0 + TZ + 4 >= g.pnz - np || (!g.fs && z0 - 4 <= np);
 }
 
 // u = staggered d/dx of p at u-position j (fwi_2d.c:775-784); pr[c] = p[row][c].
@@ -143,8 +213,11 @@ __device__ __forceinline__ void stage_tile(const float* __restrict__ f, const Ge
     constexpr int Q = SPW / 4;
     for (int i = tid; i < SPH * Q; i += NTH) {
         const int r = i / Q, q = i - r * Q;
-        const float4 v = __ldg(reinterpret_cast<const float4*>(f + (long long)(z0 - HZ + r) * g.ld + (x0 - HX) + 4 * q));
-        *reinterpret_cast<float4*>(sp + r * SPW + 4 * q) = v;
+        const float* src = f + (long long)(z0 - HZ + r) * g.ld + (x0 - HX) + 4 * q;
+        float* dst = sp + r * SPW + 4 * q;
+        if (!FWI_ALIGNED(src, 16, "stage_tile src") || !FWI_ALIGNED(dst, 16, "stage_tile dst")) continue;
+        if (!DBG_OK(src, 16, "stage_tile global")) continue;
+        *reinterpret_cast<float4*>(dst) = __ldg(reinterpret_cast<const float4*>(src));
     }
 }
 
@@ -165,6 +238,7 @@ __device__ __forceinline__ float load_strip(const StepParams& P, const ShotDev& 
 {
     const Geo& g = P.g;
     const float* ring = P.ring + sd.ring_off + (long long)t * P.strip_len;
+    if (!DBG_OK(ring, 4, "load_strip base") || !DBG_OK(ring + P.strip_len - 1, 4, "load_strip end")) return 0.f;
     if (iz < NSTRIP) return ring[iz * g.nx + ix];
     if (iz >= g.nz - NSTRIP) return ring[(NSTRIP + g.nz - 1 - iz) * g.nx + ix];
     const float* lr = ring + 2 * NSTRIP * g.nx;
@@ -177,7 +251,7 @@ __device__ __forceinline__ float load_strip(const StepParams& P, const ShotDev& 
 // ---------------------------------------------------------------------------
 template <bool GEN>
 __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd, int s, int x0, int z0,
-                                         float* sp, float* su, float* vals)
+                                         float* sp, float* su)
 {
     const Geo& g = P.g;
     const Coef& cf = P.c;
@@ -334,21 +408,20 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                     }
                 }
             }
-            float pn = 0.f;
             if (!GEN || (row < g.pnz && c < g.pnx)) {
                 const long long o = (long long)row * g.ld + c;
                 const float kk = __ldg(K + o);
-                pn = fmaf(kk, ux + vz, fmaf(2.f, pc[i + 3], -pold[o]));      // fwi_2d.c:878
+                float pn = fmaf(kk, ux + vz, fmaf(2.f, pc[i + 3], -pold[o]));      // fwi_2d.c:878
                 if (row == sd.src_r && c == sd.src_c) pn += amp * kk;
                 pold[o] = pn;
-                if (GEN) save_strip(P, sd, row, c, pn, P.step);
+                save_strip(P, sd, row, c, pn, P.step);
             }
-            vals[h * R + i] = pn;
         }
     }
 }
 
-__global__ void __launch_bounds__(NTH) k_forward(const StepParams P)
+// Forward step, tiles of the general path (edges, CPML, strips).
+__global__ void __launch_bounds__(NTH) k_fwd_gen(const StepParams P)
 {
     __shared__ __align__(16) float sp[SPH * SPW];
     __shared__ __align__(16) float su[TZ * UWP];
@@ -356,42 +429,88 @@ __global__ void __launch_bounds__(NTH) k_forward(const StepParams P)
     const ShotDev sd = P.shots[s];
     if (P.step >= sd.nt) return;
     const Geo& g = P.g;
-    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
-    const int tile = blockIdx.y * g.ntx + blockIdx.x;
+    const int2 t = P.gen_tiles[blockIdx.x];
+    const int x0 = t.x * TX, z0 = t.y * TZ;
     stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
     __syncthreads();
-    float vals[CX * R];
-    const bool gen = tile_general(g, x0, z0);
-    if (gen) fwd_tile<true>(P, sd, s, x0, z0, sp, su, vals);
-    else     fwd_tile<false>(P, sd, s, x0, z0, sp, su, vals);
-    if (!gen) {
-        // interior tiles can still hold strip cells when the CPML is thin
-        const int zs0 = g.z0p + NSTRIP, zs1 = g.z0p + g.nz - NSTRIP;
-        const int xs0 = g.x0p + NSTRIP, xs1 = g.x0p + g.nx - NSTRIP;
-        if (z0 < zs0 || z0 + TZ > zs1 || x0 < xs0 || x0 + TX > xs1) {
-            #pragma unroll
-            for (int h = 0; h < CX; ++h)
-                #pragma unroll
-                for (int i = 0; i < R; ++i)
-                    save_strip(P, sd, z0 + R * threadIdx.y + i, x0 + threadIdx.x + BX * h, vals[h * R + i], P.step);
-        }
-    }
-    // receiver sampling every jump steps (syn[r][k] = p^{k*jump+1})
-    const int rb = P.rtile[sd.rtile_off + tile], re = P.rtile[sd.rtile_off + tile + 1];
-    if (re > rb && (P.step % P.jump) == 0) {
-        __syncthreads();
+    fwd_tile<true>(P, sd, s, x0, z0, sp, su);
+}
+
+// Forward step, interior tiles: no edge, CPML or strip cells, so every cell
+// takes the same branch-free stencil.  The per-cell loads of p^{it-1} and K
+// are issued before the tile copy so that their latencies overlap.
+__global__ void __launch_bounds__(NTH, 4) k_fwd_fast(const StepParams P)
+{
+    __shared__ __align__(16) float sp[SPH * SPW];
+    __shared__ __align__(16) float su[TZ * UWP];
+    const int s = blockIdx.z + P.shot_base;
+    const int nt = P.shots[s].nt;
+    if (P.step >= nt) return;
+    const Geo& g = P.g;
+    const Coef& cf = P.c;
+    const int x0 = (P.fast_tx0 + blockIdx.x) * TX, z0 = (P.fast_tz0 + blockIdx.y) * TZ;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const long long so = (long long)s * g.fstride;
+    float* __restrict__ pold = P.pold + so;
+    const int r0l = R * ty, r0 = z0 + r0l;
+    float po[CX * R], kk[CX * R];
+    #pragma unroll
+    for (int h = 0; h < CX; ++h)
         #pragma unroll
-        for (int h = 0; h < CX; ++h)
-            #pragma unroll
-            for (int i = 0; i < R; ++i)
-                su[(R * threadIdx.y + i) * TX + threadIdx.x + BX * h] = vals[h * R + i];
-        __syncthreads();
-        const int k = P.step / P.jump;
-        for (int q = rb + threadIdx.y * BX + threadIdx.x; q < re; q += NTH) {
-            const RecDev rd = P.recs[q];
-            P.syn[rd.syn_base + k] = su[rd.cell];
+        for (int i = 0; i < R; ++i) {
+            const long long o = (long long)(r0 + i) * g.ld + x0 + tx + BX * h;
+            po[h * R + i] = __ldcg(pold + o);
+            kk[h * R + i] = __ldg(P.K + o);
+        }
+    stage_tile(P.pcur + so, g, x0, z0, sp);
+    __syncthreads();
+    #pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int rl = ty + BY * k;
+        const float* pr = sp + (rl + HZ) * SPW + HX - x0;
+        #pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            const int jj = tx + BX * h;
+            if (jj >= UW) break;
+            const int j = x0 - 1 + jj;
+            su[rl * UWP + jj] = cf.c0x * (pr[j] - pr[j - 1]) + cf.c1x * (pr[j + 1] - pr[j - 2]);
         }
     }
+    __syncthreads();
+    const ShotDev sd = P.shots[s];
+    const float amp = P.wav[sd.wav_off + P.step] * cf.iarea;
+    #pragma unroll
+    for (int h = 0; h < CX; ++h) {
+        const int cl = tx + BX * h, c = x0 + cl;
+        float pc[R + 6];
+        #pragma unroll
+        for (int k = 0; k < R + 6; ++k) pc[k] = sp[(r0l + k) * SPW + HX + cl];
+        float vv[R + 3];
+        #pragma unroll
+        for (int k = 0; k < R + 3; ++k) vv[k] = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int row = r0 + i;
+            const float* ur = su + (r0l + i) * UWP + 1 - x0;
+            const float vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
+            const float ux = cf.c0x * (ur[c + 1] - ur[c]) + cf.c1x * (ur[c + 2] - ur[c - 1]);
+            const float k1 = kk[h * R + i];
+            float pn = fmaf(k1, ux + vz, fmaf(2.f, pc[i + 3], -po[h * R + i]));
+            if (row == sd.src_r && c == sd.src_c) pn += amp * k1;
+            __stcg(pold + (long long)row * g.ld + c, pn);
+        }
+    }
+}
+
+// syn[r][it/jump] = p^{it+1}(receiver r) for every receiver of the launched shots.
+__global__ void k_sample(const RecParams Q)
+{
+    const int i = Q.lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Q.hi) return;
+    if (!FWI_ALIGNED(Q.recs + i, 8, "k_sample rec")) return;
+    const RecSample r = Q.recs[i];
+    if (Q.step >= Q.shots[r.slot].nt) return;
+    Q.syn[r.syn_base + Q.step / Q.jump] = Q.field[(long long)r.slot * Q.g.fstride + r.foff];
 }
 
 // ---------------------------------------------------------------------------
@@ -624,7 +743,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
 
 __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
 {
-    extern __shared__ __align__(16) unsigned char smraw[];
+    FWI_DYN_SMEM(smraw);
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = P.shots[s];
@@ -659,7 +778,7 @@ __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
     __syncthreads();
 
     float bm[CX * R];
-    if (tile_general(g, x0, z0)) adj_tile<true>(P, sd, s, x0, z0, sm, do_res, bm);
+    if (tile_x_general(g, x0) || tile_z_general(g, z0)) adj_tile<true>(P, sd, s, x0, z0, sm, do_res, bm);
     else                         adj_tile<false>(P, sd, s, x0, z0, sm, do_res, bm);
     if (!phys) return;   // uniform per block
 

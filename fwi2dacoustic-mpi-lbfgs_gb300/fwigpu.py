@@ -18,7 +18,9 @@ import os
 import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libfwigpu.so")
+# FWI_LIB selects another build of the same ABI (the CPU emulation build used
+# by the memory-safety tests); by default the sm_103a library is loaded.
+LIB_PATH = os.environ.get("FWI_LIB", os.path.join(PKG, "libfwigpu.so"))
 
 FWI_OK = 0
 STATUS = {0: "FWI_OK", -1: "FWI_ERR_ARG", -2: "FWI_ERR_GEOMETRY", -3: "FWI_ERR_NOMEM", -4: "FWI_ERR_CUDA",
