@@ -114,11 +114,17 @@ class Clocks:
 
 
 def traffic_per_cell_step(kernel):
+    """DRAM bytes per physical cell-step of one launch of `kernel`, as measured
+    by ncu (profiles/traffic.txt: lines of `kernel bytes`)."""
     try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            return float(json.load(f)[kernel]["dram_bytes_per_cell_step"])
-    except Exception:
-        return None
+        with open(os.path.join(ROOT, "profiles", "traffic.txt")) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 2 and parts[0] == kernel:
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
 
 
 def workload(args):
