@@ -188,7 +188,7 @@ typedef void* cudaStream_t;
 typedef void* cudaEvent_t;
 typedef void* cudaGraph_t;
 typedef void* cudaGraphExec_t;
-enum { cudaSuccess = 0, cudaErrorNotSupported = 801 };
+enum { cudaSuccess = 0, cudaErrorInvalidDevice = 101, cudaErrorNotSupported = 801 };
 enum cudaMemcpyKind { cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost, cudaMemcpyDeviceToDevice };
 enum { cudaStreamNonBlocking = 1 };
 enum cudaStreamCaptureMode { cudaStreamCaptureModeThreadLocal };
@@ -200,6 +200,8 @@ inline cudaError_t cudaGetLastError() { return cudaSuccess; }
 inline cudaError_t cudaGetDeviceCount(int* n) { *n = 1; return cudaSuccess; }
 inline cudaError_t cudaGetDeviceProperties(cudaDeviceProp* p, int) { *p = cudaDeviceProp{}; return cudaSuccess; }
 inline cudaError_t cudaSetDevice(int) { return cudaSuccess; }
+inline cudaError_t cudaGetDevice(int* d) { *d = 0; return cudaSuccess; }
+template <class T> inline cudaError_t cudaGetSymbolAddress(void** p, T& sym) { *p = (void*)&sym; return cudaSuccess; }
 template <class T> inline cudaError_t cudaMalloc(T** p, size_t n)
 {
     *p = (T*)std::malloc(n ? n : 1);

@@ -10,12 +10,18 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
 
 using namespace fwi;
+
+// Scratch of fwi_l2_misfit_noalloc: one FP64 sum of squares per trace.  It
+// lives in the library image, so every device that loads the library holds
+// these 512 KB until the process exits; no call ever allocates.
+static __device__ __align__(256) double g_noalloc_trace_sums[FWI_NOALLOC_MAX_TRACES];
 
 namespace {
 
@@ -846,6 +852,41 @@ int fwi_gradient_f32(fwi_ctx* x, double* misfit, float* grad_out)
 }
 
 const double* fwi_grad_device(const fwi_ctx* x) { return x ? x->grad : nullptr; }
+
+// Device address of g_noalloc_trace_sums for each device, looked up once per
+// device with that device current (host code cannot use the symbol itself).
+static double* noalloc_scratch(int device, cudaError_t* err)
+{
+    static std::mutex m;
+    static double* addr[64] = {};
+    *err = cudaSuccess;
+    if (device < 0 || device >= 64) { *err = cudaErrorInvalidDevice; return nullptr; }
+    std::lock_guard<std::mutex> lk(m);
+    if (!addr[device]) {
+        double* p = nullptr;
+        *err = cudaGetSymbolAddress((void**)&p, g_noalloc_trace_sums);
+        if (*err != cudaSuccess) return nullptr;
+        addr[device] = p;
+    }
+    return addr[device];
+}
+
+int fwi_l2_misfit_noalloc(const float* syn, const float* obs, float* residual, int ntraces, int nsamples,
+                          double* misfit, void* stream)
+{
+    if (!syn || !obs || !residual || !misfit || ntraces < 1 || nsamples < 1) return FWI_ERR_ARG;
+    if (ntraces > FWI_NOALLOC_MAX_TRACES) return FWI_ERR_ARG;   // beyond the static scratch
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return FWI_ERR_NODEVICE; }
+    cudaError_t e = cudaSuccess;
+    double* part = noalloc_scratch(dev, &e);
+    if (!part) { cudaGetLastError(); return FWI_ERR_CUDA; }
+    cudaStream_t st = (cudaStream_t)stream;
+    FWI_LAUNCH(k_misfit_traces, ntraces, 256, 0, st, syn, obs, residual, nsamples, part);
+    FWI_LAUNCH(k_misfit_final, 1, 256, 0, st, part, ntraces, misfit);
+    if (cudaGetLastError() != cudaSuccess) return FWI_ERR_CUDA;
+    return FWI_OK;
+}
 
 int fwi_set_stream(fwi_ctx* x, void* stream)
 {

@@ -885,6 +885,29 @@ __global__ void k_misfit(const float* __restrict__ syn, const float* __restrict_
     }
 }
 
+// Per-trace variant of k_misfit: block t forms res = syn - obs for trace t
+// and writes sum(res^2) of that trace (FP64) to partial[t].
+__global__ void k_misfit_traces(const float* __restrict__ syn, const float* __restrict__ obs, float* __restrict__ res,
+                                int nsamples, double* __restrict__ partial)
+{
+    __shared__ double ws[32];
+    const long long base = (long long)blockIdx.x * nsamples;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nsamples; i += blockDim.x) {
+        const float r = syn[base + i] - obs[base + i];
+        res[base + i] = r;
+        acc += (double)r * (double)r;
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) partial[blockIdx.x] = v;
+    }
+}
+
 // out[0] = out[1] = 1/2 sum partial (deterministic single-block sum).
 __global__ void k_misfit_final(const double* __restrict__ partial, int n, double* __restrict__ out)
 {

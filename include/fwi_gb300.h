@@ -142,6 +142,32 @@ const char *fwi_status_string(int status);
 const char *fwi_last_error(const fwi_ctx *ctx);   /* detail of the last failure */
 int fwi_version(void);
 
+/* ---- allocation-free entry point --------------------------------------- */
+/* No counterpart in the reference: an addition for callers that must not
+ * allocate device memory.  Some callers cannot call cudaMalloc: their
+ * device memory belongs to another allocator (a framework's memory pool
+ * that owns the whole budget), or they sit in a tight loop where
+ * cudaMalloc/cudaFree would stall them by synchronising the device.
+ *
+ * The per-trace L2 misfit of traces already on the device, as the misfit
+ * step of fwi_gradient computes it, using only caller-owned buffers:
+ *   residual = syn - obs          (device, ntraces x nsamples, trace-major)
+ *   misfit[0] = misfit[1] = 1/2 sum residual^2   (device, 2 doubles, FP64)
+ * The per-trace FP64 partial sums live in a fixed scratch array inside the
+ * library (FWI_NOALLOC_MAX_TRACES doubles = 512 KB per device, held from
+ * when the library is loaded until the process exits); ntraces above that
+ * limit returns FWI_ERR_ARG.  Work is queued on `stream` (a cudaStream_t of
+ * the current device, NULL for the default stream) and the call returns
+ * without waiting.  The first call on each device looks up the scratch
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  Every call on a device uses the same scratch array, so calls
+ * whose work overlaps on the GPU (different streams without ordering, or
+ * other threads) race and must be serialised by the caller.  Each call
+ * overwrites the scratch entries it reads, so nothing needs clearing. */
+#define FWI_NOALLOC_MAX_TRACES 65536
+int fwi_l2_misfit_noalloc(const float *syn, const float *obs, float *residual, int ntraces, int nsamples,
+                          double *misfit, void *stream);
+
 /* ---- host-only helpers (no device needed) ------------------------------ */
 /* Validates a configuration without touching a device. */
 int fwi_check_config(const fwi_config *cfg);
