@@ -42,7 +42,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     tmp = LIB + ".tmp"
     cmd = [nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
            "-I", os.path.join(ROOT, "include"), "-o", tmp] + SOURCES
-    # FWI_NVCC_EXTRA adds diagnostics flags, e.g. -DFWI_ALIGN_CHECK
+    # FWI_NVCC_EXTRA adds diagnostics flags, e.g. -DFWI_SELF_CHECK
     cmd[1:1] = os.environ.get("FWI_NVCC_EXTRA", "").split()
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
@@ -70,6 +70,7 @@ def build_emu(force: bool = False, sanitize: bool = True) -> str:
            "-Wno-unknown-pragmas", "-I", os.path.join(ROOT, "include"), "-o", EMU_LIB + ".tmp"] + SOURCES + ["-lpthread"]
     if sanitize:
         cmd[1:1] = ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer"]
+    cmd[1:1] = os.environ.get("FWI_EMU_EXTRA", "").split()     # e.g. -DFWI_SELF_CHECK
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("emulation build failed:\n" + r.stdout + r.stderr)

@@ -54,6 +54,11 @@ template <class T> inline T __ldg(const T* p) { return *p; }
 template <class T> inline T __ldcg(const T* p) { return *p; }
 template <class T> inline void __stcg(T* p, T v) { *p = v; }
 inline float atomicAdd(float* p, float v) { return std::atomic_ref<float>(*p).fetch_add(v); }
+inline int atomicCAS(int* p, int cmp, int val)
+{
+    std::atomic_ref<int>(*p).compare_exchange_strong(cmp, val);
+    return cmp;
+}
 
 namespace fwi_emu {
 
@@ -202,6 +207,8 @@ inline cudaError_t cudaGetDeviceProperties(cudaDeviceProp* p, int) { *p = cudaDe
 inline cudaError_t cudaSetDevice(int) { return cudaSuccess; }
 inline cudaError_t cudaGetDevice(int* d) { *d = 0; return cudaSuccess; }
 template <class T> inline cudaError_t cudaGetSymbolAddress(void** p, T& sym) { *p = (void*)&sym; return cudaSuccess; }
+template <class T> inline cudaError_t cudaMemcpyToSymbol(T& sym, const void* src, size_t n) { std::memcpy(&sym, src, n); return cudaSuccess; }
+template <class T> inline cudaError_t cudaMemcpyFromSymbol(void* dst, const T& sym, size_t n) { std::memcpy(dst, &sym, n); return cudaSuccess; }
 template <class T> inline cudaError_t cudaMalloc(T** p, size_t n)
 {
     *p = (T*)std::malloc(n ? n : 1);

@@ -208,13 +208,21 @@ int active_slots(const fwi_ctx* x, int pred_ge)   // shots with nt >= pred_ge
     return n;
 }
 
-// FWI_ALIGN_CHECK builds synchronise after every launch and name the kernel
-// that failed (diagnostics only).
-#ifdef FWI_ALIGN_CHECK
-#define DIAG_SYNC(tag)                                                                        \
-    do {                                                                                      \
-        cudaError_t e_ = cudaStreamSynchronize(x->st);                                       \
-        if (e_ != cudaSuccess) { fprintf(stderr, "FWI diag: %s failed: %s\n", tag, cudaGetErrorString(e_)); } \
+// FWI_SELF_CHECK builds (diagnostics only) synchronise after every launch,
+// name the kernel that failed and report the first access that the kernels'
+// own checks redirected (g_check: source line, index or address, block).
+#ifdef FWI_SELF_CHECK
+#define DIAG_SYNC(tag)                                                                                 \
+    do {                                                                                               \
+        cudaError_t e_ = cudaStreamSynchronize(x->st);                                                \
+        if (e_ != cudaSuccess) fprintf(stderr, "FWI diag: %s failed: %s\n", tag, cudaGetErrorString(e_)); \
+        CheckRec c_{};                                                                                 \
+        if (cudaMemcpyFromSymbol(&c_, g_check, sizeof(c_)) == cudaSuccess && c_.bad) {               \
+            fprintf(stderr, "FWI check: %s line %d idx %lld lim %lld blk %d,%d,%d thr %d,%d\n", tag,  \
+                    c_.site, c_.idx, c_.lim, c_.bx, c_.by, c_.bz, c_.tx, c_.ty);                       \
+            c_ = CheckRec{};                                                                           \
+            cudaMemcpyToSymbol(g_check, &c_, sizeof(c_));                                             \
+        }                                                                                              \
     } while (0)
 #else
 #define DIAG_SYNC(tag) do {} while (0)
@@ -267,9 +275,12 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
 long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
 {
     P.shot_base = lo;
-    FWI_LAUNCH(k_backward, dim3(x->g.ntx, x->g.ntz, hi - lo), dim3(BX, BY), sizeof(BwdSmem), x->st, P);
-    DIAG_SYNC("k_backward");
-    return 1;
+    const dim3 grid(x->g.ntx, x->g.ntz, hi - lo);
+    FWI_LAUNCH(k_backward<BWD_INTERIOR>, grid, dim3(BX, BY), sizeof(BwdSmem), x->st, P);
+    DIAG_SYNC("k_backward<BWD_INTERIOR>");
+    FWI_LAUNCH(k_backward<BWD_EDGE>, grid, dim3(BX, BY), sizeof(BwdSmem), x->st, P);
+    DIAG_SYNC("k_backward<BWD_EDGE>");
+    return 2;
 }
 
 int run_forward(fwi_ctx* x)
@@ -555,7 +566,10 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     if (cudaMemsetAsync(x->K, 0, sizeof(float) * g.fstride, x->st) != cudaSuccess ||
         cudaStreamSynchronize(x->st) != cudaSuccess)
         return bail(FWI_ERR_CUDA);
-    if (cudaFuncSetAttribute(k_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BwdSmem)) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_backward<BWD_INTERIOR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(BwdSmem)) != cudaSuccess ||
+        cudaFuncSetAttribute(k_backward<BWD_EDGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(BwdSmem)) != cudaSuccess)
         return bail(FWI_ERR_CUDA);
     if (status) *status = FWI_OK;
     return x;
@@ -720,7 +734,7 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     CK(cudaMemcpyAsync(x->rtile_d, rt_all.data(), sizeof(int) * rt_all.size(), cudaMemcpyHostToDevice, x->st));
     CK(cudaMemcpyAsync(x->wav, wav_all.data(), sizeof(float) * wav_all.size(), cudaMemcpyHostToDevice, x->st));
     CK(cudaMemsetAsync(x->syn, 0, sizeof(float) * std::max<long long>(1, syn_off), x->st));
-#ifdef FWI_ALIGN_CHECK
+#ifdef FWI_SELF_CHECK
     {
         DbgRanges r{};
         auto add = [&](const void* p, size_t bytes) {
@@ -811,7 +825,11 @@ static int gradient_impl(fwi_ctx* x, double* misfit)
     CK(cudaSetDevice(x->cfg.device));
     x->have_fwd = false;
     CK(cudaEventRecord(x->ev[6], x->st));
+#ifdef FWI_SELF_CHECK
+    const bool graph = false;          // DIAG_SYNC synchronises after every launch
+#else
     const bool graph = x->cfg.use_graph != 0;
+#endif
     int s = run_phase(x, PH_FWD, graph);
     if (!s) s = run_phase(x, PH_MIS, graph);
     if (!s) s = run_phase(x, PH_BWD, graph);

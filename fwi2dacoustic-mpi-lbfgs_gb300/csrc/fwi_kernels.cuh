@@ -38,41 +38,59 @@
 
 namespace fwi {
 
-// FWI_ALIGN_CHECK builds (diagnostics only) verify the alignment of every
-// vector or asynchronous access, report the offending address and skip it.
-#ifdef FWI_ALIGN_CHECK
-#define FWI_ALIGNED(ptr, n, tag)                                                                   \
-    ((((unsigned long long)(ptr)) % (n)) == 0 ||                                                   \
-     (printf("FWI misaligned %s: %p (mod %d = %llu) blk %d,%d,%d thr %d,%d\n", tag, (void*)(ptr), \
-             (int)(n), ((unsigned long long)(ptr)) % (n), blockIdx.x, blockIdx.y, blockIdx.z,     \
-             threadIdx.x, threadIdx.y), false))
-#else
-#define FWI_ALIGNED(ptr, n, tag) true
-#endif
-
-// Allocation table for FWI_ALIGN_CHECK builds: every checked access must fall
-// inside one of these [lo, hi) byte ranges and be aligned to its size.
+// Self-checking diagnostics build (FWI_SELF_CHECK, never the product build):
+// every shared-memory index goes through SIDX and every global pointer that
+// is dereferenced through GP.  A shared index outside its array or a global
+// access outside the registered allocations (or misaligned for its type) is
+// recorded once in g_check (site = source line) and redirected to a valid
+// dummy location, so a checked kernel cannot fault.  Product builds compile
+// both macros to the plain expression.
 struct DbgRanges {
     unsigned long long lo[24], hi[24];
     int n;
 };
-#ifdef FWI_ALIGN_CHECK
+struct CheckRec {
+    int bad, site;
+    long long idx, lim;
+    int bx, by, bz, tx, ty;
+};
+#ifdef FWI_SELF_CHECK
 __device__ DbgRanges g_dbg;
-__device__ inline bool dbg_ok(const void* p, int bytes, const char* tag)
+__device__ CheckRec g_check;
+__device__ __align__(16) float g_sink[16];
+__device__ inline void check_record(int site, long long idx, long long lim)
+{
+    if (atomicCAS(&g_check.bad, 0, 1) == 0) {
+        g_check.site = site;
+        g_check.idx = idx;
+        g_check.lim = lim;
+        g_check.bx = blockIdx.x; g_check.by = blockIdx.y; g_check.bz = blockIdx.z;
+        g_check.tx = threadIdx.x; g_check.ty = threadIdx.y;
+    }
+}
+__device__ inline int sidx(int i, int n, int site)
+{
+    if ((unsigned)i < (unsigned)n) return i;
+    check_record(site, i, n);
+    return 0;
+}
+template <class T>
+__device__ inline T* gptr(T* p, int site)
 {
     const unsigned long long a = (unsigned long long)p;
+    const unsigned long long al = sizeof(T) >= 16 ? 16 : sizeof(T);
     bool in = false;
     for (int i = 0; i < g_dbg.n; ++i)
-        if (a >= g_dbg.lo[i] && a + bytes <= g_dbg.hi[i]) { in = true; break; }
-    const bool al = (a % (unsigned long long)(bytes > 16 ? 16 : bytes)) == 0;
-    if (!in || !al)
-        printf("FWI bad access %s: %p (%d B) in=%d aligned=%d blk %d,%d,%d thr %d,%d\n", tag, p, bytes, (int)in,
-               (int)al, blockIdx.x, blockIdx.y, blockIdx.z, threadIdx.x, threadIdx.y);
-    return in && al;
+        if (a >= g_dbg.lo[i] && a + sizeof(T) <= g_dbg.hi[i]) { in = true; break; }
+    if (in && a % al == 0) return p;
+    check_record(site, (long long)a, in ? -2 : -1);   // lim -1: outside every allocation, -2: misaligned
+    return reinterpret_cast<T*>(g_sink);
 }
-#define DBG_OK(p, bytes, tag) dbg_ok((p), (bytes), (tag))
+#define SIDX(i, n) ::fwi::sidx((i), (n), __LINE__)
+#define GP(p) ::fwi::gptr((p), __LINE__)
 #else
-#define DBG_OK(p, bytes, tag) true
+#define SIDX(i, n) (i)
+#define GP(p) (p)
 #endif
 
 constexpr int TX = 64;             // tile width  (cells)
@@ -213,11 +231,8 @@ __device__ __forceinline__ void stage_tile(const float* __restrict__ f, const Ge
     constexpr int Q = SPW / 4;
     for (int i = tid; i < SPH * Q; i += NTH) {
         const int r = i / Q, q = i - r * Q;
-        const float* src = f + (long long)(z0 - HZ + r) * g.ld + (x0 - HX) + 4 * q;
-        float* dst = sp + r * SPW + 4 * q;
-        if (!FWI_ALIGNED(src, 16, "stage_tile src") || !FWI_ALIGNED(dst, 16, "stage_tile dst")) continue;
-        if (!DBG_OK(src, 16, "stage_tile global")) continue;
-        *reinterpret_cast<float4*>(dst) = __ldg(reinterpret_cast<const float4*>(src));
+        const float4* src = reinterpret_cast<const float4*>(f + (long long)(z0 - HZ + r) * g.ld + (x0 - HX) + 4 * q);
+        *reinterpret_cast<float4*>(sp + SIDX(r * SPW + 4 * q, SPH * SPW)) = __ldg(GP(src));
     }
 }
 
@@ -238,12 +253,11 @@ __device__ __forceinline__ float load_strip(const StepParams& P, const ShotDev& 
 {
     const Geo& g = P.g;
     const float* ring = P.ring + sd.ring_off + (long long)t * P.strip_len;
-    if (!DBG_OK(ring, 4, "load_strip base") || !DBG_OK(ring + P.strip_len - 1, 4, "load_strip end")) return 0.f;
-    if (iz < NSTRIP) return ring[iz * g.nx + ix];
-    if (iz >= g.nz - NSTRIP) return ring[(NSTRIP + g.nz - 1 - iz) * g.nx + ix];
+    if (iz < NSTRIP) return *GP(ring + iz * g.nx + ix);
+    if (iz >= g.nz - NSTRIP) return *GP(ring + (NSTRIP + g.nz - 1 - iz) * g.nx + ix);
     const float* lr = ring + 2 * NSTRIP * g.nx;
-    if (ix < NSTRIP) return lr[ix * g.nz + iz];
-    return lr[(NSTRIP + g.nx - 1 - ix) * g.nz + iz];
+    if (ix < NSTRIP) return *GP(lr + ix * g.nz + iz);
+    return *GP(lr + (NSTRIP + g.nx - 1 - ix) * g.nz + iz);
 }
 
 // ---------------------------------------------------------------------------
@@ -507,7 +521,6 @@ __global__ void k_sample(const RecParams Q)
 {
     const int i = Q.lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Q.hi) return;
-    if (!FWI_ALIGNED(Q.recs + i, 8, "k_sample rec")) return;
     const RecSample r = Q.recs[i];
     if (Q.step >= Q.shots[r.slot].nt) return;
     Q.syn[r.syn_base + Q.step / Q.jump] = Q.field[(long long)r.slot * Q.g.fstride + r.foff];
@@ -524,6 +537,9 @@ struct BwdSmem {
     float racc[TZ * TX];   // receiver adjoint sources of the tile
 };
 
+// All shared-memory accesses below use integer indices relative to the start
+// of their array (global column jg of the tile row sits at jg - x0 + offset),
+// so no pointer is ever formed outside the array it points into.
 template <bool GEN>
 __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd, int s, int x0, int z0,
                                          BwdSmem& sm, bool do_res, float* bm)
@@ -539,35 +555,36 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     const float* a1x = a0x + 2 * n2;    const float* b1x = a0x + 3 * n2;
     const float* a0z = a0x + 4 * n2;    const float* b0z = a0x + 5 * n2;
     const float* a1z = a0x + 6 * n2;    const float* b1z = a0x + 7 * n2;
+    [[maybe_unused]] constexpr int NS = SPH * SPW, NU = TZ * UWP, NR = TZ * RXP;
 
     // x stage 1 (general tiles): rbar = q adjusted by the adjoint of the ux psi recursion
     if (GEN) {
         #pragma unroll
         for (int k = 0; k < R; ++k) {
             const int rl = ty + BY * k, row = z0 + rl;
-            const float* qr = sm.sq + (rl + HZ) * SPW + HX - x0;
+            const int qrow = (rl + HZ) * SPW + HX - 3;        // sq index of column x0 - 3
             #pragma unroll
             for (int h = 0; h < 3; ++h) {
                 const int ii = tx + BX * h;
                 if (ii >= RXW) break;
                 const int i = x0 - 3 + ii;
-                float r = qr[i];
+                float r = sm.sq[SIDX(qrow + ii, NS)];
                 if (row < pnz && i >= 0 && i < pnx) {
                     const bool own = ii >= 3 && ii < 3 + TX;
                     if (i < np) {
                         const int idx = P.pl.ux0 + row * np + i;
-                        const float t = r + psr[idx];
-                        r = r + a0x[2 * i + 1] * t;
-                        if (own) psw[idx] = b0x[2 * i + 1] * t;
+                        const float t = r + *GP(psr + idx);
+                        r = r + *GP(a0x + 2 * i + 1) * t;
+                        if (own) *GP(psw + idx) = *GP(b0x + 2 * i + 1) * t;
                     } else if (i >= pnx - np) {
                         const int kk = i - (pnx - np);
                         const int idx = P.pl.ux1 + row * np + kk;
-                        const float t = r + psr[idx];
-                        r = r + a1x[2 * kk + 1] * t;
-                        if (own) psw[idx] = b1x[2 * kk + 1] * t;
+                        const float t = r + *GP(psr + idx);
+                        r = r + *GP(a1x + 2 * kk + 1) * t;
+                        if (own) *GP(psw + idx) = *GP(b1x + 2 * kk + 1) * t;
                     }
                 }
-                sm.srx[rl * RXP + ii] = r;
+                sm.srx[SIDX(rl * RXP + ii, NR)] = r;
             }
         }
         __syncthreads();
@@ -583,34 +600,35 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             const int j = x0 - 1 + jj;
             float ub;
             if (!GEN) {
-                const float* qr = sm.sq + (rl + HZ) * SPW + HX - x0;
-                ub = cf.c0x * (qr[j - 1] - qr[j]) + cf.c1x * (qr[j - 2] - qr[j + 1]);
+                const int q0 = (rl + HZ) * SPW + HX - 1 + jj;     // sq index of column j
+                ub = cf.c0x * (sm.sq[SIDX(q0 - 1, NS)] - sm.sq[SIDX(q0, NS)]) +
+                     cf.c1x * (sm.sq[SIDX(q0 - 2, NS)] - sm.sq[SIDX(q0 + 1, NS)]);
             } else {
-                const float* rr = sm.srx + rl * RXP + 3 - x0;     // rr[i] = rbar[row][i]
-                #define RM(i) (((i) >= 1 && (i) <= pnx - 2) ? rr[i] : 0.f)
+                const int rbase = rl * RXP + 3 - x0;             // + global column = srx index
+                #define RM(i) (((i) >= 1 && (i) <= pnx - 2) ? sm.srx[SIDX(rbase + (i), NR)] : 0.f)
                 ub = cf.c0x * (RM(j - 1) - RM(j)) + cf.c1x * (RM(j - 2) - RM(j + 1));
                 #undef RM
-                if (j == 1) ub += cf.ix * rr[0];
-                if (j == 0) ub -= cf.ix * rr[0];
-                if (j == pnx) ub += cf.ix * rr[pnx - 1];
-                if (j == pnx - 1) ub -= cf.ix * rr[pnx - 1];
+                if (j == 1) ub += cf.ix * sm.srx[SIDX(rbase, NR)];
+                if (j == 0) ub -= cf.ix * sm.srx[SIDX(rbase, NR)];
+                if (j == pnx) ub += cf.ix * sm.srx[SIDX(rbase + pnx - 1, NR)];
+                if (j == pnx - 1) ub -= cf.ix * sm.srx[SIDX(rbase + pnx - 1, NR)];
                 if (row < pnz) {
                     const bool own = jj >= 1 && jj <= TX;
                     if (j >= 0 && j <= np) {
                         const int idx = P.pl.u0 + row * (np + 1) + j;
-                        const float t = ub + psr[idx];
-                        ub = ub + a0x[2 * j] * t;
-                        if (own) psw[idx] = b0x[2 * j] * t;
+                        const float t = ub + *GP(psr + idx);
+                        ub = ub + *GP(a0x + 2 * j) * t;
+                        if (own) *GP(psw + idx) = *GP(b0x + 2 * j) * t;
                     } else if (j >= pnx - np && j <= pnx) {
                         const int kk = j - (pnx - np);
                         const int idx = P.pl.u1 + row * (np + 1) + kk;
-                        const float t = ub + psr[idx];
-                        ub = ub + a1x[2 * kk] * t;
-                        if (own) psw[idx] = b1x[2 * kk] * t;
+                        const float t = ub + *GP(psr + idx);
+                        ub = ub + *GP(a1x + 2 * kk) * t;
+                        if (own) *GP(psw + idx) = *GP(b1x + 2 * kk) * t;
                     }
                 }
             }
-            sm.su[rl * UWP + jj] = ub;
+            sm.su[SIDX(rl * UWP + jj, NU)] = ub;
         }
     }
     __syncthreads();
@@ -623,7 +641,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         const int cl = tx + BX * h, c = x0 + cl;
         float qc[R + 6];
         #pragma unroll
-        for (int k = 0; k < R + 6; ++k) qc[k] = sm.sq[(r0l + k) * SPW + HX + cl];   // rows r0-3+k
+        for (int k = 0; k < R + 6; ++k) qc[k] = sm.sq[SIDX((r0l + k) * SPW + HX + cl, NS)];   // rows r0-3+k
         float rz[R + 6];
         #pragma unroll
         for (int k = 0; k < R + 6; ++k) {
@@ -635,14 +653,14 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                     if (row >= pnz - np) {
                         const int kk = row - (pnz - np);
                         const int idx = P.pl.vz1 + kk * pnx + c;
-                        const float t = r + psr[idx];
-                        r = r + a1z[2 * kk + 1] * t;
-                        if (own) psw[idx] = b1z[2 * kk + 1] * t;
+                        const float t = r + *GP(psr + idx);
+                        r = r + *GP(a1z + 2 * kk + 1) * t;
+                        if (own) *GP(psw + idx) = *GP(b1z + 2 * kk + 1) * t;
                     } else if (!g.fs && row < np) {
                         const int idx = P.pl.vz0 + row * pnx + c;
-                        const float t = r + psr[idx];
-                        r = r + a0z[2 * row + 1] * t;
-                        if (own) psw[idx] = b0z[2 * row + 1] * t;
+                        const float t = r + *GP(psr + idx);
+                        r = r + *GP(a0z + 2 * row + 1) * t;
+                        if (own) *GP(psw + idx) = *GP(b0z + 2 * row + 1) * t;
                     }
                 }
             }
@@ -664,8 +682,9 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 v = cf.c0z * (m1 - m0) + cf.c1z * (m2 - p1);
                 if (g.fs) {
                     if (kv >= 0 && kv <= 4) {
-                        // vz[0] = (-22 v0 + 17 v1 + 9 v2 - 5 v3 + v4) iz24 (fwi_2d.c:848), transposed
-                        const float r00 = sm.sq[(HZ - z0) * SPW + HX + cl];   // rbar[0] = q[0] (no top CPML)
+                        // vz[0] = (-22 v0 + 17 v1 + 9 v2 - 5 v3 + v4) iz24 (fwi_2d.c:848), transposed;
+                        // kv <= 4 only happens in the top tile (z0 == 0), where row 0 is sq row HZ
+                        const float r00 = sm.sq[SIDX(HZ * SPW + HX + cl, NS)];   // rbar[0] = q[0] (no top CPML)
                         const float hcoef = (kv == 0) ? -22.f : (kv == 1) ? 17.f : (kv == 2) ? 9.f : (kv == 3) ? -5.f : 1.f;
                         v += hcoef * r00 * cf.iz24;
                     }
@@ -680,14 +699,14 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                     if (kv >= pnz - np) {
                         const int kk = kv - (pnz - np);
                         const int idx = P.pl.v1 + kk * pnx + c;
-                        const float t = v + psr[idx];
-                        v = v + a1z[2 * kk] * t;
-                        if (own) psw[idx] = b1z[2 * kk] * t;
+                        const float t = v + *GP(psr + idx);
+                        v = v + *GP(a1z + 2 * kk) * t;
+                        if (own) *GP(psw + idx) = *GP(b1z + 2 * kk) * t;
                     } else if (!g.fs && kv <= np) {
                         const int idx = P.pl.v0 + kv * pnx + c;
-                        const float t = v + psr[idx];
-                        v = v + a0z[2 * kv] * t;
-                        if (own) psw[idx] = b0z[2 * kv] * t;
+                        const float t = v + *GP(psr + idx);
+                        v = v + *GP(a0z + 2 * kv) * t;
+                        if (own) *GP(psw + idx) = *GP(b0z + 2 * kv) * t;
                     }
                 }
             }
@@ -696,11 +715,12 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i;
-            const float* ub = sm.su + (r0l + i) * UWP + 1 - x0;              // ub[j] = ubar[row][j]
+            const int ubase = (r0l + i) * UWP + 1 - x0;                   // + u position = su index
+            #define UB(j) sm.su[SIDX(ubase + (j), NU)]
             float pz, px;
             if (!GEN) {
                 pz = cf.c0z * (vb[i + 1] - vb[i + 2]) + cf.c1z * (vb[i] - vb[i + 3]);
-                px = cf.c0x * (ub[c] - ub[c + 1]) + cf.c1x * (ub[c - 1] - ub[c + 2]);
+                px = cf.c0x * (UB(c) - UB(c + 1)) + cf.c1x * (UB(c - 1) - UB(c + 2));
             } else {
                 // vbar index of row q is q - (r0 - 1)
                 const float M0 = (row     >= 2 && row     <= pnz - 2) ? vb[i + 1] : 0.f;
@@ -720,41 +740,52 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 }
                 if (row == pnz - 1) pz += cf.iz * vb[i + 1];
                 if (row == pnz - 2) pz -= cf.iz * vb[i + 2];
-                #define UM(j) (((j) >= 2 && (j) <= pnx - 2) ? ub[j] : 0.f)
+                #define UM(j) (((j) >= 2 && (j) <= pnx - 2) ? UB(j) : 0.f)
                 px = cf.c0x * (UM(c) - UM(c + 1)) + cf.c1x * (UM(c - 1) - UM(c + 2));
                 #undef UM
-                if (c == 1) px += cf.ix * ub[1];
-                if (c == 0) px -= cf.ix * ub[1];
-                if (c == pnx - 1) px += cf.ix * ub[pnx - 1];
-                if (c == pnx - 2) px -= cf.ix * ub[pnx - 1];
+                if (c == 1) px += cf.ix * UB(1);
+                if (c == 0) px -= cf.ix * UB(1);
+                if (c == pnx - 1) px += cf.ix * UB(pnx - 1);
+                if (c == pnx - 2) px -= cf.ix * UB(pnx - 1);
             }
+            #undef UB
             float pbar = px + pz;
-            if (do_res) pbar += sm.racc[(r0l + i) * TX + cl];
+            if (do_res) pbar += sm.racc[SIDX((r0l + i) * TX + cl, TZ * TX)];
             float b = 0.f;
             if (!GEN || (row < pnz && c < pnx)) {
                 const long long o = (long long)row * g.ld + c;
-                b = fmaf(__ldg(K + o), pbar, fmaf(2.f, qc[i + 3], -bold[o]));
-                bold[o] = b;
+                b = fmaf(__ldg(GP(K + o)), pbar, fmaf(2.f, qc[i + 3], -*GP(bold + o)));
+                *GP(bold + o) = b;
             }
             bm[h * R + i] = b;
         }
     }
 }
 
+// Tile classes of the backward step.  BWD_INTERIOR tiles (no edge, CPML or
+// strip cell in reach of their stencils) and BWD_EDGE tiles (all others) run
+// as two instantiations, so that the interior one carries none of the edge
+// code's registers; BWD_ALL runs every tile in one launch.
+enum { BWD_ALL = 0, BWD_INTERIOR = 1, BWD_EDGE = 2 };
+
+template <int CLS>
 __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
 {
     FWI_DYN_SMEM(smraw);
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
+    const Geo& g = P.g;
+    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
+    const bool gen = tile_x_general(g, x0) || tile_z_general(g, z0);
+    if ((CLS == BWD_INTERIOR && gen) || (CLS == BWD_EDGE && !gen)) return;   // uniform per block
     const int s = blockIdx.z + P.shot_base;
-    const ShotDev sd = P.shots[s];
+    const ShotDev sd = *GP(P.shots + s);
     const int m = P.step;
     if (m > sd.nt) return;
-    const Geo& g = P.g;
     const Coef& cf = P.c;
-    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
     const int tile = blockIdx.y * g.ntx + blockIdx.x;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
     const long long so = (long long)s * g.fstride;
+    [[maybe_unused]] constexpr int NS = SPH * SPW, NU = TZ * UWP;
 
     // physical region and the rebuilt interior (3 cells inside it)
     const int zp0 = g.z0p, zp1 = g.z0p + g.nz, xp0 = g.x0p, xp1 = g.x0p + g.nx;
@@ -764,22 +795,22 @@ __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
     if (phys) stage_tile(P.pcur + so, g, x0, z0, sm.sp);
 
     // adjoint sources r^m at the receivers when m-1 = k*jump
-    const int rb = P.rtile[sd.rtile_off + tile], re = P.rtile[sd.rtile_off + tile + 1];
+    const int rb = *GP(P.rtile + sd.rtile_off + tile), re = *GP(P.rtile + sd.rtile_off + tile + 1);
     const bool do_res = re > rb && ((m - 1) % P.jump) == 0;
     if (do_res) {
-        for (int q = tid; q < TZ * TX; q += NTH) sm.racc[q] = 0.f;
+        for (int q = tid; q < TZ * TX; q += NTH) sm.racc[SIDX(q, TZ * TX)] = 0.f;
         __syncthreads();
         const int k = (m - 1) / P.jump;
         for (int q = rb + tid; q < re; q += NTH) {
-            const RecDev rd = P.recs[q];
-            atomicAdd(&sm.racc[rd.cell], P.res[rd.syn_base + k]);
+            const RecDev rd = *GP(P.recs + q);
+            atomicAdd(&sm.racc[SIDX(rd.cell, TZ * TX)], *GP(P.res + rd.syn_base + k));
         }
     }
     __syncthreads();
 
     float bm[CX * R];
-    if (tile_x_general(g, x0) || tile_z_general(g, z0)) adj_tile<true>(P, sd, s, x0, z0, sm, do_res, bm);
-    else                         adj_tile<false>(P, sd, s, x0, z0, sm, do_res, bm);
+    if (CLS == BWD_EDGE || (CLS == BWD_ALL && gen)) adj_tile<true>(P, sd, s, x0, z0, sm, do_res, bm);
+    else                                           adj_tile<false>(P, sd, s, x0, z0, sm, do_res, bm);
     if (!phys) return;   // uniform per block
 
     // rebuild of p^{m-2} and imaging
@@ -787,13 +818,13 @@ __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
     #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int rl = ty + BY * k;
-        const float* pr = sm.sp + (rl + HZ) * SPW + HX - x0;
         #pragma unroll
         for (int h = 0; h < 3; ++h) {
             const int jj = tx + BX * h;
             if (jj >= UW) break;
-            const int j = x0 - 1 + jj;
-            sm.su[rl * UWP + jj] = cf.c0x * (pr[j] - pr[j - 1]) + cf.c1x * (pr[j + 1] - pr[j - 2]);
+            const int p0 = (rl + HZ) * SPW + HX - 1 + jj;      // sp index of column j = x0 - 1 + jj
+            sm.su[SIDX(rl * UWP + jj, NU)] = cf.c0x * (sm.sp[SIDX(p0, NS)] - sm.sp[SIDX(p0 - 1, NS)]) +
+                                             cf.c1x * (sm.sp[SIDX(p0 + 1, NS)] - sm.sp[SIDX(p0 - 2, NS)]);
         }
     }
     __syncthreads();
@@ -801,31 +832,33 @@ __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
     const float* __restrict__ K = P.K;
     float* __restrict__ pold = P.pold + so;
     float* __restrict__ gacc = P.gacc + so;
-    const float f = P.wav[sd.wav_off + m - 1] * cf.iarea;
+    const float f = *GP(P.wav + sd.wav_off + m - 1) * cf.iarea;
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
         const int cl = tx + BX * h, c = x0 + cl;
         const int ix = c - g.x0p;
-        if (ix < 0 || ix >= g.nx) continue;
+        if (CLS != BWD_INTERIOR && (ix < 0 || ix >= g.nx)) continue;
         float pc[R + 6];
         #pragma unroll
-        for (int k = 0; k < R + 6; ++k) pc[k] = sm.sp[(r0l + k) * SPW + HX + cl];
+        for (int k = 0; k < R + 6; ++k) pc[k] = sm.sp[SIDX((r0l + k) * SPW + HX + cl, NS)];
         float vv[R + 3];
         #pragma unroll
         for (int k = 0; k < R + 3; ++k) vv[k] = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i, iz = row - g.z0p;
-            if (iz < 0 || iz >= g.nz) continue;
+            if (CLS != BWD_INTERIOR && (iz < 0 || iz >= g.nz)) continue;
             const long long o = (long long)row * g.ld + c;
-            const float kk = __ldg(K + o);
-            const float pm = pold[o];            // p^m
+            const float kk = __ldg(GP(K + o));
+            const float pm = *GP(pold + o);      // p^m
             const float p1 = pc[i + 3];          // p^{m-1}
             float pn, lp;
-            if (iz >= NSTRIP && iz < g.nz - NSTRIP && ix >= NSTRIP && ix < g.nx - NSTRIP) {
-                const float* ur = sm.su + (r0l + i) * UWP + 1 - x0;
+            // interior tiles hold no strip cell
+            if (CLS == BWD_INTERIOR || (iz >= NSTRIP && iz < g.nz - NSTRIP && ix >= NSTRIP && ix < g.nx - NSTRIP)) {
+                const int u0 = (r0l + i) * UWP + 1 + cl;        // su index of u position c
                 const float vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
-                const float ux = cf.c0x * (ur[c + 1] - ur[c]) + cf.c1x * (ur[c + 2] - ur[c - 1]);
+                const float ux = cf.c0x * (sm.su[SIDX(u0 + 1, NU)] - sm.su[SIDX(u0, NU)]) +
+                                 cf.c1x * (sm.su[SIDX(u0 + 2, NU)] - sm.su[SIDX(u0 - 1, NU)]);
                 const float w = ux + vz;
                 pn = fmaf(kk, w, fmaf(2.f, p1, -pm));
                 lp = w;
@@ -834,8 +867,8 @@ __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
                 pn = (m - 3 >= 0) ? load_strip(P, sd, iz, ix, m - 3) : 0.f;
                 lp = ((pm - 2.f * p1) + pn) / kk;
             }
-            pold[o] = pn;
-            gacc[o] = fmaf(bm[h * R + i], lp, gacc[o]);
+            *GP(pold + o) = pn;
+            *GP(gacc + o) = fmaf(bm[h * R + i], lp, *GP(gacc + o));
         }
     }
 }

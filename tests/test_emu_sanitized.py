@@ -1,0 +1,58 @@
+"""Memory safety of the CUDA kernels without a GPU.
+
+The engine's own .cu source is compiled as C++ against csrc/cpu_emu.h
+(every CUDA block runs on host threads, every device buffer is an exact-size
+heap block, dynamic shared memory is exactly the launch's byte count) under
+AddressSanitizer and UBSan.  One gradient per boundary condition then runs
+through the C ABI of that build in a child process: any out-of-bounds access
+in any kernel aborts it.  The results must also match the FP64 oracle to the
+GPU parity tolerances, so the emulation runs the same arithmetic.
+"""
+import json
+import os
+import shutil
+import subprocess
+import sys
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GRAD_TOL = 1e-4
+SYN_TOL = 2e-5
+
+
+def _sanitizer_libs():
+    cxx = shutil.which(os.environ.get("CXX", "g++"))
+    if not cxx:
+        return None
+    libs = []
+    for name in ("libasan.so", "libubsan.so"):
+        p = subprocess.run([cxx, f"-print-file-name={name}"], capture_output=True, text=True).stdout.strip()
+        if not os.path.isabs(p) or not os.path.exists(p):
+            return None
+        libs.append(p)
+    return libs
+
+
+@pytest.fixture(scope="module")
+def emu_lib():
+    libs = _sanitizer_libs()
+    if libs is None:
+        pytest.skip("g++ with AddressSanitizer/UBSan runtimes not available")
+    import build as B
+    return B.build_emu(), libs
+
+
+@pytest.mark.parametrize("fs", [1, 0])
+def test_emulated_gradient_is_memory_safe_and_matches_oracle(emu_lib, oracles, fs):
+    lib, libs = emu_lib
+    env = dict(os.environ, FWI_LIB=lib, LD_PRELOAD=" ".join(libs),
+               ASAN_OPTIONS="detect_leaks=0:abort_on_error=1", UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1")
+    r = subprocess.run([sys.executable, os.path.join(HERE, "emu_gradient_case.py"), str(fs), "61"],
+                       capture_output=True, text=True, env=env, timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-6000:]
+    assert "ERROR: AddressSanitizer" not in r.stderr and "runtime error" not in r.stderr, r.stderr[-6000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["syn_rel"] <= SYN_TOL, out
+    assert abs(out["J"] - out["J64"]) <= 1e-5 * out["J64"], out
+    assert out["grad_rel"] <= GRAD_TOL, out
