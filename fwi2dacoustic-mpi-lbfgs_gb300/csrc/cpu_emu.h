@@ -195,7 +195,7 @@ typedef void* cudaGraph_t;
 typedef void* cudaGraphExec_t;
 enum { cudaSuccess = 0, cudaErrorInvalidDevice = 101, cudaErrorNotSupported = 801 };
 enum cudaMemcpyKind { cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost, cudaMemcpyDeviceToDevice };
-enum { cudaStreamNonBlocking = 1 };
+enum { cudaStreamNonBlocking = 1, cudaEventDisableTiming = 2 };
 enum cudaStreamCaptureMode { cudaStreamCaptureModeThreadLocal };
 enum cudaFuncAttribute { cudaFuncAttributeMaxDynamicSharedMemorySize };
 struct cudaDeviceProp { int major = 10, minor = 3; };
@@ -223,6 +223,8 @@ inline cudaError_t cudaStreamCreateWithFlags(cudaStream_t* s, int) { *s = (void*
 inline cudaError_t cudaStreamDestroy(cudaStream_t) { return cudaSuccess; }
 inline cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }
 inline cudaError_t cudaEventCreate(cudaEvent_t* e) { *e = (void*)0x1; return cudaSuccess; }
+inline cudaError_t cudaEventCreateWithFlags(cudaEvent_t* e, int) { *e = (void*)0x1; return cudaSuccess; }
+inline cudaError_t cudaStreamWaitEvent(cudaStream_t, cudaEvent_t, int) { return cudaSuccess; }
 inline cudaError_t cudaEventDestroy(cudaEvent_t) { return cudaSuccess; }
 inline cudaError_t cudaEventRecord(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
 inline cudaError_t cudaEventElapsedTime(float* ms, cudaEvent_t, cudaEvent_t) { *ms = 0.f; return cudaSuccess; }

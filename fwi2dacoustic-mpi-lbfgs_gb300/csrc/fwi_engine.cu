@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <mutex>
 #include <cstdio>
 #include <cstring>
@@ -75,6 +76,12 @@ struct fwi_ctx {
     cudaStream_t own = nullptr;    // the context's stream
     cudaStream_t st = nullptr;     // stream in use (own, or the caller's)
     cudaEvent_t ev[8]{};           // [0,1] forward, [2,3] backward, [4,5] misfit, [6,7] whole call
+    // The general-tile classes of a step run on side streams, forked from and
+    // joined back into st around every step, concurrently with the interior
+    // tiles (they write disjoint cells and read the same inputs).  A captured
+    // graph keeps them as parallel branches.
+    cudaStream_t side[3]{};
+    cudaEvent_t fork_ev = nullptr, join_ev[3]{};
     cudaGraph_t graph[3]{};        // captured phases (use_graph): forward, misfit, backward
     cudaGraphExec_t gexec[3]{};
     long long graph_launches[3]{};
@@ -107,8 +114,9 @@ struct fwi_ctx {
     RecSample* samp_d = nullptr;   // receivers, slot order (forward sampling)
     RecDev* recs_d = nullptr;      // receivers grouped by tile (backward injection)
     int* rtile_d = nullptr;        // per-slot, per-tile CSR of recs_d
-    int2* gen_d = nullptr;         // tiles of the general path
+    int2* gen_d = nullptr;         // tiles of the general path, grouped by class (GX only, GZ only, both)
     int ngen = 0;
+    int gen_off[4] = {};           // class c occupies gen_d[gen_off[c], gen_off[c + 1])
     int ftx0 = 0, ftx1 = 0, ftz0 = 0, ftz1 = 0;   // interior tile rectangle
     std::vector<int> samp_off;                    // per-slot ranges (nshots + 1)
     std::vector<int> nt_slot;      // nt of each slot, descending
@@ -241,24 +249,66 @@ RecParams rec_params(const fwi_ctx* x, float* field, int step)
     return Q;
 }
 
-// One forward step of the shots [lo, hi): interior tiles, general tiles,
-// then receiver sampling.
+// Stream of general-tile class cls.  Self-checking builds keep every launch
+// on st so that DIAG_SYNC sees each kernel finish.
+#ifdef FWI_SELF_CHECK
+constexpr bool kConcurrentClasses = false;
+#else
+constexpr bool kConcurrentClasses = true;
+#endif
+
+cudaStream_t class_stream(const fwi_ctx* x, int cls) { return kConcurrentClasses ? x->side[cls] : x->st; }
+
+// Forks the side streams of the non-empty classes from st.
+void fork_classes(fwi_ctx* x)
+{
+    if (!kConcurrentClasses) return;
+    cudaEventRecord(x->fork_ev, x->st);
+    for (int cls = 0; cls < 3; ++cls)
+        if (x->gen_off[cls + 1] > x->gen_off[cls]) cudaStreamWaitEvent(x->side[cls], x->fork_ev, 0);
+}
+
+// Joins them back: st waits for every class launched since the fork.
+void join_classes(fwi_ctx* x)
+{
+    if (!kConcurrentClasses) return;
+    for (int cls = 0; cls < 3; ++cls)
+        if (x->gen_off[cls + 1] > x->gen_off[cls]) {
+            cudaEventRecord(x->join_ev[cls], x->side[cls]);
+            cudaStreamWaitEvent(x->st, x->join_ev[cls], 0);
+        }
+}
+
+// One forward step of the shots [lo, hi): general tiles (one launch per
+// class, on the side streams) and interior tiles concurrently, then receiver
+// sampling.
 long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
 {
     const dim3 block(BX, BY);
     const int n = hi - lo;
     long long l = 0;
     P.shot_base = lo;
+    fork_classes(x);
+    const int2* gen = P.gen_tiles;
+    for (int cls = 0; cls < 3; ++cls) {
+        const int cnt = x->gen_off[cls + 1] - x->gen_off[cls];
+        if (!cnt) continue;
+        P.gen_tiles = x->gen_d + x->gen_off[cls];
+        const dim3 grid(cnt, 1, n);
+        cudaStream_t cs = class_stream(x, cls);
+        if (cls == 0) FWI_LAUNCH((k_fwd_gen<true, false>), grid, block, 0, cs, P);
+        if (cls == 1) FWI_LAUNCH((k_fwd_gen<false, true>), grid, block, 0, cs, P);
+        if (cls == 2) FWI_LAUNCH((k_fwd_gen<true, true>), grid, block, 0, cs, P);
+        DIAG_SYNC("k_fwd_gen");
+        ++l;
+    }
+    P.gen_tiles = gen;
     if (x->ftx1 > x->ftx0 && x->ftz1 > x->ftz0) {
         FWI_LAUNCH(k_fwd_fast, dim3(x->ftx1 - x->ftx0, x->ftz1 - x->ftz0, n), block, 0, x->st, P);
         DIAG_SYNC("k_fwd_fast");
         ++l;
     }
-    if (x->ngen) {
-        FWI_LAUNCH(k_fwd_gen, dim3(x->ngen, 1, n), block, 0, x->st, P);
-        DIAG_SYNC("k_fwd_gen");
-        ++l;
-    }
+    join_classes(x);
     if (P.step % x->cfg.jump == 0) {
         RecParams Q = rec_params(x, P.pold, P.step);
         Q.lo = x->samp_off[lo];
@@ -272,15 +322,37 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
     return l;
 }
 
+// One backward step of the shots [lo, hi): general tiles (one launch per
+// class, on the side streams) and interior tiles concurrently.
 long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
 {
+    const dim3 block(BX, BY);
+    const int n = hi - lo;
+    long long l = 0;
     P.shot_base = lo;
-    const dim3 grid(x->g.ntx, x->g.ntz, hi - lo);
-    FWI_LAUNCH(k_backward<BWD_INTERIOR>, grid, dim3(BX, BY), sizeof(BwdSmem), x->st, P);
-    DIAG_SYNC("k_backward<BWD_INTERIOR>");
-    FWI_LAUNCH(k_backward<BWD_EDGE>, grid, dim3(BX, BY), sizeof(BwdSmem), x->st, P);
-    DIAG_SYNC("k_backward<BWD_EDGE>");
-    return 2;
+    fork_classes(x);
+    // z-only tiles never touch srx (the last member of BwdSmem)
+    const int2* gen = P.gen_tiles;
+    for (int cls = 0; cls < 3; ++cls) {
+        const int cnt = x->gen_off[cls + 1] - x->gen_off[cls];
+        if (!cnt) continue;
+        P.gen_tiles = x->gen_d + x->gen_off[cls];
+        const dim3 grid(cnt, 1, n);
+        cudaStream_t cs = class_stream(x, cls);
+        if (cls == 0) FWI_LAUNCH((k_bwd_edge<true, false>), grid, block, sizeof(BwdSmem), cs, P);
+        if (cls == 1) FWI_LAUNCH((k_bwd_edge<false, true>), grid, block, offsetof(BwdSmem, srx), cs, P);
+        if (cls == 2) FWI_LAUNCH((k_bwd_edge<true, true>), grid, block, sizeof(BwdSmem), cs, P);
+        DIAG_SYNC("k_bwd_edge");
+        ++l;
+    }
+    P.gen_tiles = gen;
+    if (x->ftx1 > x->ftx0 && x->ftz1 > x->ftz0) {
+        FWI_LAUNCH(k_bwd_int, dim3(x->ftx1 - x->ftx0, x->ftz1 - x->ftz0, n), block, sizeof(BwdIntSmem), x->st, P);
+        DIAG_SYNC("k_bwd_int");
+        ++l;
+    }
+    join_classes(x);
+    return l;
 }
 
 int run_forward(fwi_ctx* x)
@@ -493,6 +565,11 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     x->st = x->own;
     for (auto& e : x->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return bail(FWI_ERR_CUDA);
+    for (int i = 0; i < 3; ++i)
+        if (cudaStreamCreateWithFlags(&x->side[i], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&x->join_ev[i], cudaEventDisableTiming) != cudaSuccess)
+            return bail(FWI_ERR_CUDA);
+    if (cudaEventCreateWithFlags(&x->fork_ev, cudaEventDisableTiming) != cudaSuccess) return bail(FWI_ERR_CUDA);
 
     Geo& g = x->g;
     g.nx = cfg->nx; g.nz = cfg->nz; g.npml = cfg->npml; g.fs = cfg->free_surface;
@@ -515,9 +592,19 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
         for (int t = 0; t < g.ntz; ++t)
             if (!tile_z_general(g, t * TZ)) { if (tz0 < 0) tz0 = t; tz1 = t + 1; }
         if (tx0 < 0 || tz0 < 0) tx0 = tx1 = tz0 = tz1 = 0;
-        for (int tz = 0; tz < g.ntz; ++tz)
-            for (int tx = 0; tx < g.ntx; ++tx)
-                if (!(tx >= tx0 && tx < tx1 && tz >= tz0 && tz < tz1)) gen.push_back(make_int2(tx, tz));
+        // general tiles grouped by class: 0 = x-general only, 1 = z-general only, 2 = both
+        for (int cls = 0; cls < 3; ++cls) {
+            x->gen_off[cls] = (int)gen.size();
+            for (int tz = 0; tz < g.ntz; ++tz)
+                for (int tx = 0; tx < g.ntx; ++tx) {
+                    if (tx >= tx0 && tx < tx1 && tz >= tz0 && tz < tz1) continue;
+                    const bool gx = tile_x_general(g, tx * TX), gz = tile_z_general(g, tz * TZ);
+                    if (!gx && !gz) return bail(FWI_ERR_ARG);     // cannot happen: such tiles form the rectangle
+                    if ((gx && !gz && cls == 0) || (!gx && gz && cls == 1) || (gx && gz && cls == 2))
+                        gen.push_back(make_int2(tx, tz));
+                }
+        }
+        x->gen_off[3] = (int)gen.size();
         x->ftx0 = tx0; x->ftx1 = tx1; x->ftz0 = tz0; x->ftz1 = tz1;
         x->ngen = (int)gen.size();
         if (dalloc(x, &x->gen_d, gen.size(), &x->bytes_model)) return bail(FWI_ERR_NOMEM);
@@ -566,9 +653,13 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     if (cudaMemsetAsync(x->K, 0, sizeof(float) * g.fstride, x->st) != cudaSuccess ||
         cudaStreamSynchronize(x->st) != cudaSuccess)
         return bail(FWI_ERR_CUDA);
-    if (cudaFuncSetAttribute(k_backward<BWD_INTERIOR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_bwd_int, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BwdIntSmem)) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_bwd_edge<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(BwdSmem)) != cudaSuccess ||
-        cudaFuncSetAttribute(k_backward<BWD_EDGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_bwd_edge<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(BwdSmem)) != cudaSuccess ||
+        cudaFuncSetAttribute(k_bwd_edge<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(BwdSmem)) != cudaSuccess)
         return bail(FWI_ERR_CUDA);
     if (status) *status = FWI_OK;
@@ -582,6 +673,9 @@ void fwi_destroy(fwi_ctx* x)
     void* ps[] = {x->K, x->vel, x->pmlc, x->grad, x->gradf, x->gen_d};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& e : x->ev) if (e) cudaEventDestroy(e);
+    for (auto& e : x->join_ev) if (e) cudaEventDestroy(e);
+    if (x->fork_ev) cudaEventDestroy(x->fork_ev);
+    for (auto& t : x->side) if (t) cudaStreamDestroy(t);
     if (x->own) cudaStreamDestroy(x->own);
     delete x;
 }

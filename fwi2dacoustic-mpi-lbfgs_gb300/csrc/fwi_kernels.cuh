@@ -214,12 +214,16 @@ __host__ __device__ inline bool tile_z_general(const Geo& g, int z0)
     return z0 < 8 || z0 + TZ + 8 > g.pnz || z0 + TZ + 4 >= g.pnz - np || (!g.fs && z0 - 4 <= np);
 }
 
-// u = staggered d/dx of p at u-position j (fwi_2d.c:775-784); pr[c] = p[row][c].
-__device__ __forceinline__ float u_edge(const float* pr, int j, int pnx, const Coef& c)
+// u = staggered d/dx of p at u-position j (fwi_2d.c:775-784); p[row][col]
+// is sp[base + col] (base = row offset - x0 + HX, an integer, so no pointer
+// leaves the array).
+__device__ __forceinline__ float u_edge(const float* sp, int base, int j, int pnx, const Coef& c)
 {
-    if (j >= 2 && j <= pnx - 2) return c.c0x * (pr[j] - pr[j - 1]) + c.c1x * (pr[j + 1] - pr[j - 2]);
-    if (j == 1) return c.ix * (pr[1] - pr[0]);
-    if (j == pnx - 1) return c.ix * (pr[pnx - 1] - pr[pnx - 2]);
+    #define PX(col) sp[SIDX(base + (col), SPH * SPW)]
+    if (j >= 2 && j <= pnx - 2) return c.c0x * (PX(j) - PX(j - 1)) + c.c1x * (PX(j + 1) - PX(j - 2));
+    if (j == 1) return c.ix * (PX(1) - PX(0));
+    if (j == pnx - 1) return c.ix * (PX(pnx - 1) - PX(pnx - 2));
+    #undef PX
     return 0.f;   // u[0], u[pnx] are never assigned by the reference
 }
 
@@ -242,11 +246,11 @@ __device__ __forceinline__ void save_strip(const StepParams& P, const ShotDev& s
     const int iz = row - g.z0p, ix = c - g.x0p;
     if (iz < 0 || iz >= g.nz || ix < 0 || ix >= g.nx) return;
     float* ring = P.ring + sd.ring_off + (long long)t * P.strip_len;
-    if (iz < NSTRIP) ring[iz * g.nx + ix] = val;
-    if (iz >= g.nz - NSTRIP) ring[(NSTRIP + g.nz - 1 - iz) * g.nx + ix] = val;
+    if (iz < NSTRIP) *GP(ring + iz * g.nx + ix) = val;
+    if (iz >= g.nz - NSTRIP) *GP(ring + (NSTRIP + g.nz - 1 - iz) * g.nx + ix) = val;
     float* lr = ring + 2 * NSTRIP * g.nx;
-    if (ix < NSTRIP) lr[ix * g.nz + iz] = val;
-    if (ix >= g.nx - NSTRIP) lr[(NSTRIP + g.nx - 1 - ix) * g.nz + iz] = val;
+    if (ix < NSTRIP) *GP(lr + ix * g.nz + iz) = val;
+    if (ix >= g.nx - NSTRIP) *GP(lr + (NSTRIP + g.nx - 1 - ix) * g.nz + iz) = val;
 }
 
 __device__ __forceinline__ float load_strip(const StepParams& P, const ShotDev& sd, int iz, int ix, int t)
@@ -263,7 +267,13 @@ __device__ __forceinline__ float load_strip(const StepParams& P, const ShotDev& 
 // ---------------------------------------------------------------------------
 // Forward step
 // ---------------------------------------------------------------------------
-template <bool GEN>
+// One forward tile.  GX / GZ select the general (edge, CPML and strip aware)
+// formulas along x / z; an axis whose general flag is false takes the plain
+// interior stencil, which the tile classification (tile_x_general,
+// tile_z_general) guarantees to be exact there.  In tiles that reach past the
+// padded grid, warps whose rows all lie beyond pnz and column halves beyond
+// pnx skip their work (uniform per warp).
+template <bool GX, bool GZ>
 __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd, int s, int x0, int z0,
                                          float* sp, float* su)
 {
@@ -283,54 +293,57 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
     #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int rl = ty + BY * k, row = z0 + rl;
-        const float* pr = sp + (rl + HZ) * SPW + HX - x0;
+        if (GZ && row >= g.pnz) continue;                                   // rows past the grid
+        const int pbase = (rl + HZ) * SPW + HX - x0;                       // + global column = sp index
         #pragma unroll
         for (int h = 0; h < 3; ++h) {
             const int jj = tx + BX * h;
             if (jj >= UW) break;
             const int j = x0 - 1 + jj;
             float u;
-            if (!GEN) {
-                u = cf.c0x * (pr[j] - pr[j - 1]) + cf.c1x * (pr[j + 1] - pr[j - 2]);
+            if (!GX) {
+                const int q = pbase + j;
+                u = cf.c0x * (sp[SIDX(q, SPH * SPW)] - sp[SIDX(q - 1, SPH * SPW)]) +
+                    cf.c1x * (sp[SIDX(q + 1, SPH * SPW)] - sp[SIDX(q - 2, SPH * SPW)]);
             } else {
-                u = u_edge(pr, j, g.pnx, cf);
-                if (row < g.pnz) {
-                    const bool own = jj >= 1 && jj <= TX;
-                    if (j >= 0 && j <= np) {                               // fwi_2d.c:790-791
-                        const int idx = P.pl.u0 + row * (np + 1) + j;
-                        const float ps = b0x[2 * j] * psr[idx] + a0x[2 * j] * u;
-                        if (own) psw[idx] = ps;
-                        u += ps;
-                    } else if (j >= g.pnx - np && j <= g.pnx) {           // fwi_2d.c:793-794
-                        const int kk = j - (g.pnx - np);
-                        const int idx = P.pl.u1 + row * (np + 1) + kk;
-                        const float ps = b1x[2 * kk] * psr[idx] + a1x[2 * kk] * u;
-                        if (own) psw[idx] = ps;
-                        u += ps;
-                    }
+                u = u_edge(sp, pbase, j, g.pnx, cf);
+                const bool own = jj >= 1 && jj <= TX;
+                if (j >= 0 && j <= np) {                                   // fwi_2d.c:790-791
+                    const int idx = P.pl.u0 + row * (np + 1) + j;
+                    const float ps = *GP(b0x + 2 * j) * *GP(psr + idx) + *GP(a0x + 2 * j) * u;
+                    if (own) *GP(psw + idx) = ps;
+                    u += ps;
+                } else if (j >= g.pnx - np && j <= g.pnx) {               // fwi_2d.c:793-794
+                    const int kk = j - (g.pnx - np);
+                    const int idx = P.pl.u1 + row * (np + 1) + kk;
+                    const float ps = *GP(b1x + 2 * kk) * *GP(psr + idx) + *GP(a1x + 2 * kk) * u;
+                    if (own) *GP(psw + idx) = ps;
+                    u += ps;
                 }
             }
-            su[rl * UWP + jj] = u;
+            su[SIDX(rl * UWP + jj, TZ * UWP)] = u;
         }
     }
     __syncthreads();
 
     const int r0l = R * ty, r0 = z0 + r0l;
+    if (GZ && r0 >= g.pnz) return;                                         // the last phase: no barrier follows
     const float* __restrict__ K = P.K;
     float* __restrict__ pold = P.pold + so;
-    const float amp = P.wav[sd.wav_off + P.step] * cf.iarea;
+    const float amp = *GP(P.wav + sd.wav_off + P.step) * cf.iarea;
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
+        if (GX && x0 + BX * h >= g.pnx) continue;                          // column half past the grid
         const int cl = tx + BX * h, c = x0 + cl;
         float pc[R + 6];
         #pragma unroll
-        for (int k = 0; k < R + 6; ++k) pc[k] = sp[(r0l + k) * SPW + HX + cl];   // rows r0-3+k
+        for (int k = 0; k < R + 6; ++k) pc[k] = sp[SIDX((r0l + k) * SPW + HX + cl, SPH * SPW)];   // rows r0-3+k
         float vv[R + 3];                                                            // v rows r0-1+k
         #pragma unroll
         for (int k = 0; k < R + 3; ++k) {
             const int kv = r0 - 1 + k;
             float v;
-            if (!GEN) {
+            if (!GZ) {
                 v = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
             } else {
                 if (kv >= 2 && kv <= g.pnz - 2) {
@@ -345,18 +358,18 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                 } else {
                     v = 0.f;
                 }
-                if (c < g.pnx && kv >= 0 && kv <= g.pnz) {
+                if ((!GX || c < g.pnx) && kv >= 0 && kv <= g.pnz) {
                     const bool own = k >= 1 && k <= R && kv < g.pnz;
                     if (kv >= g.pnz - np) {                               // fwi_2d.c:816-817
                         const int kk = kv - (g.pnz - np);
                         const int idx = P.pl.v1 + kk * g.pnx + c;
-                        const float ps = b1z[2 * kk] * psr[idx] + a1z[2 * kk] * v;
-                        if (own) psw[idx] = ps;
+                        const float ps = *GP(b1z + 2 * kk) * *GP(psr + idx) + *GP(a1z + 2 * kk) * v;
+                        if (own) *GP(psw + idx) = ps;
                         v += ps;
                     } else if (!g.fs && kv <= np) {                       // top layer, all-sides CPML
                         const int idx = P.pl.v0 + kv * g.pnx + c;
-                        const float ps = b0z[2 * kv] * psr[idx] + a0z[2 * kv] * v;
-                        if (own) psw[idx] = ps;
+                        const float ps = *GP(b0z + 2 * kv) * *GP(psr + idx) + *GP(a0z + 2 * kv) * v;
+                        if (own) *GP(psw + idx) = ps;
                         v += ps;
                     }
                 }
@@ -366,11 +379,11 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i;
-            const float* ur = su + (r0l + i) * UWP + 1 - x0;                // ur[j] = u[row][j]
+            const int ubase = (r0l + i) * UWP + 1 - x0;                     // + u position = su index
+            #define UR(j) su[SIDX(ubase + (j), TZ * UWP)]
             float vz, ux;
-            if (!GEN) {
+            if (!GZ) {
                 vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
-                ux = cf.c0x * (ur[c + 1] - ur[c]) + cf.c1x * (ur[c + 2] - ur[c - 1]);
             } else {
                 if (row >= 1 && row <= g.pnz - 2) {
                     vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
@@ -386,68 +399,78 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                 } else {
                     vz = 0.f;
                 }
+            }
+            if (!GX) {
+                ux = cf.c0x * (UR(c + 1) - UR(c)) + cf.c1x * (UR(c + 2) - UR(c - 1));
+            } else {
                 if (c >= 1 && c <= g.pnx - 2) {
-                    ux = cf.c0x * (ur[c + 1] - ur[c]) + cf.c1x * (ur[c + 2] - ur[c - 1]);
+                    ux = cf.c0x * (UR(c + 1) - UR(c)) + cf.c1x * (UR(c + 2) - UR(c - 1));
                 } else if (c == 0) {                                      // fwi_2d.c:829
-                    ux = (ur[1] - ur[0]) * cf.ix;
+                    ux = (UR(1) - UR(0)) * cf.ix;
                 } else if (c == g.pnx - 1) {                              // fwi_2d.c:831
-                    ux = (ur[g.pnx] - ur[g.pnx - 1]) * cf.ix;
+                    ux = (UR(g.pnx) - UR(g.pnx - 1)) * cf.ix;
                 } else {
                     ux = 0.f;
                 }
-                if (row < g.pnz && c < g.pnx) {
-                    if (c < np) {                                         // fwi_2d.c:838-839
-                        const int idx = P.pl.ux0 + row * np + c;
-                        const float ps = b0x[2 * c + 1] * psr[idx] + a0x[2 * c + 1] * ux;
-                        psw[idx] = ps;
-                        ux += ps;
-                    } else if (c >= g.pnx - np) {                         // fwi_2d.c:841-842
-                        const int kk = c - (g.pnx - np);
-                        const int idx = P.pl.ux1 + row * np + kk;
-                        const float ps = b1x[2 * kk + 1] * psr[idx] + a1x[2 * kk + 1] * ux;
-                        psw[idx] = ps;
-                        ux += ps;
-                    }
-                    if (row >= g.pnz - np) {                              // fwi_2d.c:860-861
-                        const int kk = row - (g.pnz - np);
-                        const int idx = P.pl.vz1 + kk * g.pnx + c;
-                        const float ps = b1z[2 * kk + 1] * psr[idx] + a1z[2 * kk + 1] * vz;
-                        psw[idx] = ps;
-                        vz += ps;
-                    } else if (!g.fs && row < np) {
-                        const int idx = P.pl.vz0 + row * g.pnx + c;
-                        const float ps = b0z[2 * row + 1] * psr[idx] + a0z[2 * row + 1] * vz;
-                        psw[idx] = ps;
-                        vz += ps;
-                    }
+            }
+            #undef UR
+            const bool inside = (!GZ || row < g.pnz) && (!GX || c < g.pnx);
+            if (GX && inside) {
+                if (c < np) {                                             // fwi_2d.c:838-839
+                    const int idx = P.pl.ux0 + row * np + c;
+                    const float ps = *GP(b0x + 2 * c + 1) * *GP(psr + idx) + *GP(a0x + 2 * c + 1) * ux;
+                    *GP(psw + idx) = ps;
+                    ux += ps;
+                } else if (c >= g.pnx - np) {                             // fwi_2d.c:841-842
+                    const int kk = c - (g.pnx - np);
+                    const int idx = P.pl.ux1 + row * np + kk;
+                    const float ps = *GP(b1x + 2 * kk + 1) * *GP(psr + idx) + *GP(a1x + 2 * kk + 1) * ux;
+                    *GP(psw + idx) = ps;
+                    ux += ps;
                 }
             }
-            if (!GEN || (row < g.pnz && c < g.pnx)) {
+            if (GZ && inside) {
+                if (row >= g.pnz - np) {                                  // fwi_2d.c:860-861
+                    const int kk = row - (g.pnz - np);
+                    const int idx = P.pl.vz1 + kk * g.pnx + c;
+                    const float ps = *GP(b1z + 2 * kk + 1) * *GP(psr + idx) + *GP(a1z + 2 * kk + 1) * vz;
+                    *GP(psw + idx) = ps;
+                    vz += ps;
+                } else if (!g.fs && row < np) {
+                    const int idx = P.pl.vz0 + row * g.pnx + c;
+                    const float ps = *GP(b0z + 2 * row + 1) * *GP(psr + idx) + *GP(a0z + 2 * row + 1) * vz;
+                    *GP(psw + idx) = ps;
+                    vz += ps;
+                }
+            }
+            if (inside) {
                 const long long o = (long long)row * g.ld + c;
-                const float kk = __ldg(K + o);
-                float pn = fmaf(kk, ux + vz, fmaf(2.f, pc[i + 3], -pold[o]));      // fwi_2d.c:878
+                const float kk = __ldg(GP(K + o));
+                float pn = fmaf(kk, ux + vz, fmaf(2.f, pc[i + 3], -*GP(pold + o)));      // fwi_2d.c:878
                 if (row == sd.src_r && c == sd.src_c) pn += amp * kk;
-                pold[o] = pn;
+                *GP(pold + o) = pn;
                 save_strip(P, sd, row, c, pn, P.step);
             }
         }
     }
 }
 
-// Forward step, tiles of the general path (edges, CPML, strips).
+// Forward step, tiles of the general path (edges, CPML, strips) of one
+// class (GX, GZ), from the list P.gen_tiles.
+template <bool GX, bool GZ>
 __global__ void __launch_bounds__(NTH) k_fwd_gen(const StepParams P)
 {
     __shared__ __align__(16) float sp[SPH * SPW];
     __shared__ __align__(16) float su[TZ * UWP];
     const int s = blockIdx.z + P.shot_base;
-    const ShotDev sd = P.shots[s];
+    const ShotDev sd = *GP(P.shots + s);
     if (P.step >= sd.nt) return;
     const Geo& g = P.g;
-    const int2 t = P.gen_tiles[blockIdx.x];
+    const int2 t = *GP(P.gen_tiles + blockIdx.x);
     const int x0 = t.x * TX, z0 = t.y * TZ;
     stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
     __syncthreads();
-    fwd_tile<true>(P, sd, s, x0, z0, sp, su);
+    fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su);
 }
 
 // Forward step, interior tiles: no edge, CPML or strip cells, so every cell
@@ -458,7 +481,7 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_fast(const StepParams P)
     __shared__ __align__(16) float sp[SPH * SPW];
     __shared__ __align__(16) float su[TZ * UWP];
     const int s = blockIdx.z + P.shot_base;
-    const int nt = P.shots[s].nt;
+    const int nt = GP(P.shots + s)->nt;
     if (P.step >= nt) return;
     const Geo& g = P.g;
     const Coef& cf = P.c;
@@ -473,45 +496,46 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_fast(const StepParams P)
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const long long o = (long long)(r0 + i) * g.ld + x0 + tx + BX * h;
-            po[h * R + i] = __ldcg(pold + o);
-            kk[h * R + i] = __ldg(P.K + o);
+            po[h * R + i] = __ldcg(GP(pold + o));
+            kk[h * R + i] = __ldg(GP(P.K + o));
         }
     stage_tile(P.pcur + so, g, x0, z0, sp);
     __syncthreads();
     #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int rl = ty + BY * k;
-        const float* pr = sp + (rl + HZ) * SPW + HX - x0;
         #pragma unroll
         for (int h = 0; h < 3; ++h) {
             const int jj = tx + BX * h;
             if (jj >= UW) break;
-            const int j = x0 - 1 + jj;
-            su[rl * UWP + jj] = cf.c0x * (pr[j] - pr[j - 1]) + cf.c1x * (pr[j + 1] - pr[j - 2]);
+            const int q = (rl + HZ) * SPW + HX - 1 + jj;                  // sp index of column j = x0 - 1 + jj
+            su[SIDX(rl * UWP + jj, TZ * UWP)] = cf.c0x * (sp[SIDX(q, SPH * SPW)] - sp[SIDX(q - 1, SPH * SPW)]) +
+                                                cf.c1x * (sp[SIDX(q + 1, SPH * SPW)] - sp[SIDX(q - 2, SPH * SPW)]);
         }
     }
     __syncthreads();
-    const ShotDev sd = P.shots[s];
-    const float amp = P.wav[sd.wav_off + P.step] * cf.iarea;
+    const ShotDev sd = *GP(P.shots + s);
+    const float amp = *GP(P.wav + sd.wav_off + P.step) * cf.iarea;
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
         const int cl = tx + BX * h, c = x0 + cl;
         float pc[R + 6];
         #pragma unroll
-        for (int k = 0; k < R + 6; ++k) pc[k] = sp[(r0l + k) * SPW + HX + cl];
+        for (int k = 0; k < R + 6; ++k) pc[k] = sp[SIDX((r0l + k) * SPW + HX + cl, SPH * SPW)];
         float vv[R + 3];
         #pragma unroll
         for (int k = 0; k < R + 3; ++k) vv[k] = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i;
-            const float* ur = su + (r0l + i) * UWP + 1 - x0;
+            const int u0 = (r0l + i) * UWP + 1 + cl;                      // su index of u position c
             const float vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
-            const float ux = cf.c0x * (ur[c + 1] - ur[c]) + cf.c1x * (ur[c + 2] - ur[c - 1]);
+            const float ux = cf.c0x * (su[SIDX(u0 + 1, TZ * UWP)] - su[SIDX(u0, TZ * UWP)]) +
+                             cf.c1x * (su[SIDX(u0 + 2, TZ * UWP)] - su[SIDX(u0 - 1, TZ * UWP)]);
             const float k1 = kk[h * R + i];
             float pn = fmaf(k1, ux + vz, fmaf(2.f, pc[i + 3], -po[h * R + i]));
             if (row == sd.src_r && c == sd.src_c) pn += amp * k1;
-            __stcg(pold + (long long)row * g.ld + c, pn);
+            __stcg(GP(pold + (long long)row * g.ld + c), pn);
         }
     }
 }
@@ -521,26 +545,32 @@ __global__ void k_sample(const RecParams Q)
 {
     const int i = Q.lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Q.hi) return;
-    const RecSample r = Q.recs[i];
-    if (Q.step >= Q.shots[r.slot].nt) return;
-    Q.syn[r.syn_base + Q.step / Q.jump] = Q.field[(long long)r.slot * Q.g.fstride + r.foff];
+    const RecSample r = *GP(Q.recs + i);
+    if (Q.step >= GP(Q.shots + r.slot)->nt) return;
+    *GP(Q.syn + r.syn_base + Q.step / Q.jump) = *GP(Q.field + (long long)r.slot * Q.g.fstride + r.foff);
 }
 
 // ---------------------------------------------------------------------------
 // Backward step: adjoint + rebuild + imaging
 // ---------------------------------------------------------------------------
+// srx is the last member: tiles without x-general work are launched with
+// offsetof(BwdSmem, srx) dynamic bytes and never touch it.
 struct BwdSmem {
     float sq[SPH * SPW];   // b^{m+1} tile + halo
     float sp[SPH * SPW];   // p^{m-1} tile + halo
     float su[TZ * UWP];    // adjoint ubar, then rebuild u
-    float srx[TZ * RXP];   // adjoint x-stage input (psi-adjusted b), general tiles
     float racc[TZ * TX];   // receiver adjoint sources of the tile
+    float srx[TZ * RXP];   // adjoint x-stage input (psi-adjusted b), x-general tiles
 };
 
 // All shared-memory accesses below use integer indices relative to the start
 // of their array (global column jg of the tile row sits at jg - x0 + offset),
 // so no pointer is ever formed outside the array it points into.
-template <bool GEN>
+//
+// One adjoint tile; GX / GZ select the general formulas along x / z as in
+// fwd_tile.  Rows past pnz and column halves past pnx are skipped (uniform
+// per warp); `live` tells the caller whether this thread's rows exist.
+template <bool GX, bool GZ>
 __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd, int s, int x0, int z0,
                                          BwdSmem& sm, bool do_res, float* bm)
 {
@@ -557,11 +587,12 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     const float* a1z = a0x + 6 * n2;    const float* b1z = a0x + 7 * n2;
     [[maybe_unused]] constexpr int NS = SPH * SPW, NU = TZ * UWP, NR = TZ * RXP;
 
-    // x stage 1 (general tiles): rbar = q adjusted by the adjoint of the ux psi recursion
-    if (GEN) {
+    // x stage 1 (x-general tiles): rbar = q adjusted by the adjoint of the ux psi recursion
+    if (GX) {
         #pragma unroll
         for (int k = 0; k < R; ++k) {
             const int rl = ty + BY * k, row = z0 + rl;
+            if (GZ && row >= pnz) continue;
             const int qrow = (rl + HZ) * SPW + HX - 3;        // sq index of column x0 - 3
             #pragma unroll
             for (int h = 0; h < 3; ++h) {
@@ -569,7 +600,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 if (ii >= RXW) break;
                 const int i = x0 - 3 + ii;
                 float r = sm.sq[SIDX(qrow + ii, NS)];
-                if (row < pnz && i >= 0 && i < pnx) {
+                if (i >= 0 && i < pnx) {
                     const bool own = ii >= 3 && ii < 3 + TX;
                     if (i < np) {
                         const int idx = P.pl.ux0 + row * np + i;
@@ -593,13 +624,14 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int rl = ty + BY * k, row = z0 + rl;
+        if (GZ && row >= pnz) continue;
         #pragma unroll
         for (int h = 0; h < 3; ++h) {
             const int jj = tx + BX * h;
             if (jj >= UW) break;
             const int j = x0 - 1 + jj;
             float ub;
-            if (!GEN) {
+            if (!GX) {
                 const int q0 = (rl + HZ) * SPW + HX - 1 + jj;     // sq index of column j
                 ub = cf.c0x * (sm.sq[SIDX(q0 - 1, NS)] - sm.sq[SIDX(q0, NS)]) +
                      cf.c1x * (sm.sq[SIDX(q0 - 2, NS)] - sm.sq[SIDX(q0 + 1, NS)]);
@@ -612,20 +644,18 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 if (j == 0) ub -= cf.ix * sm.srx[SIDX(rbase, NR)];
                 if (j == pnx) ub += cf.ix * sm.srx[SIDX(rbase + pnx - 1, NR)];
                 if (j == pnx - 1) ub -= cf.ix * sm.srx[SIDX(rbase + pnx - 1, NR)];
-                if (row < pnz) {
-                    const bool own = jj >= 1 && jj <= TX;
-                    if (j >= 0 && j <= np) {
-                        const int idx = P.pl.u0 + row * (np + 1) + j;
-                        const float t = ub + *GP(psr + idx);
-                        ub = ub + *GP(a0x + 2 * j) * t;
-                        if (own) *GP(psw + idx) = *GP(b0x + 2 * j) * t;
-                    } else if (j >= pnx - np && j <= pnx) {
-                        const int kk = j - (pnx - np);
-                        const int idx = P.pl.u1 + row * (np + 1) + kk;
-                        const float t = ub + *GP(psr + idx);
-                        ub = ub + *GP(a1x + 2 * kk) * t;
-                        if (own) *GP(psw + idx) = *GP(b1x + 2 * kk) * t;
-                    }
+                const bool own = jj >= 1 && jj <= TX;
+                if (j >= 0 && j <= np) {
+                    const int idx = P.pl.u0 + row * (np + 1) + j;
+                    const float t = ub + *GP(psr + idx);
+                    ub = ub + *GP(a0x + 2 * j) * t;
+                    if (own) *GP(psw + idx) = *GP(b0x + 2 * j) * t;
+                } else if (j >= pnx - np && j <= pnx) {
+                    const int kk = j - (pnx - np);
+                    const int idx = P.pl.u1 + row * (np + 1) + kk;
+                    const float t = ub + *GP(psr + idx);
+                    ub = ub + *GP(a1x + 2 * kk) * t;
+                    if (own) *GP(psw + idx) = *GP(b1x + 2 * kk) * t;
                 }
             }
             sm.su[SIDX(rl * UWP + jj, NU)] = ub;
@@ -634,10 +664,12 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     __syncthreads();
 
     const int r0l = R * ty, r0 = z0 + r0l;
+    if (GZ && r0 >= pnz) return;                 // no rows of this thread exist; the caller skips them too
     const float* __restrict__ K = P.K;
     float* __restrict__ bold = P.bold + so;
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
+        if (GX && x0 + BX * h >= pnx) continue;
         const int cl = tx + BX * h, c = x0 + cl;
         float qc[R + 6];
         #pragma unroll
@@ -646,9 +678,9 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         #pragma unroll
         for (int k = 0; k < R + 6; ++k) {
             float r = qc[k];
-            if (GEN) {
+            if (GZ) {
                 const int row = r0 - 3 + k;
-                if (row >= 0 && row < pnz && c < pnx) {
+                if (row >= 0 && row < pnz && (!GX || c < pnx)) {
                     const bool own = k >= 3 && k < 3 + R;
                     if (row >= pnz - np) {
                         const int kk = row - (pnz - np);
@@ -671,7 +703,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         for (int k = 0; k < R + 3; ++k) {
             const int kv = r0 - 1 + k;
             float v;
-            if (!GEN) {
+            if (!GZ) {
                 v = cf.c0z * (rz[k + 1] - rz[k + 2]) + cf.c1z * (rz[k] - rz[k + 3]);
             } else {
                 // rz index of row q is q - (r0 - 3); row kv-1 -> k+1 etc.
@@ -694,7 +726,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 }
                 if (kv == pnz) v += cf.iz * rz[k + 1];
                 if (kv == pnz - 1) v -= cf.iz * rz[k + 2];
-                if (c < pnx && kv >= 0 && kv <= pnz) {
+                if ((!GX || c < pnx) && kv >= 0 && kv <= pnz) {
                     const bool own = k >= 1 && k <= R && kv < pnz;
                     if (kv >= pnz - np) {
                         const int kk = kv - (pnz - np);
@@ -718,9 +750,8 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             const int ubase = (r0l + i) * UWP + 1 - x0;                   // + u position = su index
             #define UB(j) sm.su[SIDX(ubase + (j), NU)]
             float pz, px;
-            if (!GEN) {
+            if (!GZ) {
                 pz = cf.c0z * (vb[i + 1] - vb[i + 2]) + cf.c1z * (vb[i] - vb[i + 3]);
-                px = cf.c0x * (UB(c) - UB(c + 1)) + cf.c1x * (UB(c - 1) - UB(c + 2));
             } else {
                 // vbar index of row q is q - (r0 - 1)
                 const float M0 = (row     >= 2 && row     <= pnz - 2) ? vb[i + 1] : 0.f;
@@ -740,6 +771,10 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 }
                 if (row == pnz - 1) pz += cf.iz * vb[i + 1];
                 if (row == pnz - 2) pz -= cf.iz * vb[i + 2];
+            }
+            if (!GX) {
+                px = cf.c0x * (UB(c) - UB(c + 1)) + cf.c1x * (UB(c - 1) - UB(c + 2));
+            } else {
                 #define UM(j) (((j) >= 2 && (j) <= pnx - 2) ? UB(j) : 0.f)
                 px = cf.c0x * (UM(c) - UM(c + 1)) + cf.c1x * (UM(c - 1) - UM(c + 2));
                 #undef UM
@@ -752,7 +787,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             float pbar = px + pz;
             if (do_res) pbar += sm.racc[SIDX((r0l + i) * TX + cl, TZ * TX)];
             float b = 0.f;
-            if (!GEN || (row < pnz && c < pnx)) {
+            if ((!GZ || row < pnz) && (!GX || c < pnx)) {
                 const long long o = (long long)row * g.ld + c;
                 b = fmaf(__ldg(GP(K + o)), pbar, fmaf(2.f, qc[i + 3], -*GP(bold + o)));
                 *GP(bold + o) = b;
@@ -762,27 +797,22 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     }
 }
 
-// Tile classes of the backward step.  BWD_INTERIOR tiles (no edge, CPML or
-// strip cell in reach of their stencils) and BWD_EDGE tiles (all others) run
-// as two instantiations, so that the interior one carries none of the edge
-// code's registers; BWD_ALL runs every tile in one launch.
-enum { BWD_ALL = 0, BWD_INTERIOR = 1, BWD_EDGE = 2 };
-
-template <int CLS>
-__global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
+// Backward step, tiles of the general path (edges, CPML, strips) of one
+// class (GX, GZ), from the list P.gen_tiles.
+template <bool GX, bool GZ>
+__global__ void __launch_bounds__(NTH, 3) k_bwd_edge(const StepParams P)
 {
     FWI_DYN_SMEM(smraw);
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
     const Geo& g = P.g;
-    const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
-    const bool gen = tile_x_general(g, x0) || tile_z_general(g, z0);
-    if ((CLS == BWD_INTERIOR && gen) || (CLS == BWD_EDGE && !gen)) return;   // uniform per block
+    const int2 t = *GP(P.gen_tiles + blockIdx.x);
+    const int x0 = t.x * TX, z0 = t.y * TZ;
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
     const int m = P.step;
     if (m > sd.nt) return;
     const Coef& cf = P.c;
-    const int tile = blockIdx.y * g.ntx + blockIdx.x;
+    const int tile = t.y * g.ntx + t.x;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
     const long long so = (long long)s * g.fstride;
     [[maybe_unused]] constexpr int NS = SPH * SPW, NU = TZ * UWP;
@@ -809,15 +839,15 @@ __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
     __syncthreads();
 
     float bm[CX * R];
-    if (CLS == BWD_EDGE || (CLS == BWD_ALL && gen)) adj_tile<true>(P, sd, s, x0, z0, sm, do_res, bm);
-    else                                           adj_tile<false>(P, sd, s, x0, z0, sm, do_res, bm);
+    adj_tile<GX, GZ>(P, sd, s, x0, z0, sm, do_res, bm);
     if (!phys) return;   // uniform per block
 
-    // rebuild of p^{m-2} and imaging
+    // rebuild of p^{m-2} and imaging (physical cells only)
     __syncthreads();     // su is reused
     #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int rl = ty + BY * k;
+        if (GZ && z0 + rl >= zp1) continue;
         #pragma unroll
         for (int h = 0; h < 3; ++h) {
             const int jj = tx + BX * h;
@@ -829,15 +859,17 @@ __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
     }
     __syncthreads();
     const int r0l = R * ty, r0 = z0 + r0l;
+    if (GZ && (r0 >= zp1 || r0 + R <= zp0)) return;   // no physical row of this thread; no barrier follows
     const float* __restrict__ K = P.K;
     float* __restrict__ pold = P.pold + so;
     float* __restrict__ gacc = P.gacc + so;
     const float f = *GP(P.wav + sd.wav_off + m - 1) * cf.iarea;
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
+        if (GX && (x0 + BX * h >= xp1 || x0 + BX * h + BX <= xp0)) continue;   // no physical column in this half
         const int cl = tx + BX * h, c = x0 + cl;
         const int ix = c - g.x0p;
-        if (CLS != BWD_INTERIOR && (ix < 0 || ix >= g.nx)) continue;
+        if (GX && (ix < 0 || ix >= g.nx)) continue;
         float pc[R + 6];
         #pragma unroll
         for (int k = 0; k < R + 6; ++k) pc[k] = sm.sp[SIDX((r0l + k) * SPW + HX + cl, NS)];
@@ -847,14 +879,14 @@ __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i, iz = row - g.z0p;
-            if (CLS != BWD_INTERIOR && (iz < 0 || iz >= g.nz)) continue;
+            if (GZ && (iz < 0 || iz >= g.nz)) continue;
             const long long o = (long long)row * g.ld + c;
             const float kk = __ldg(GP(K + o));
             const float pm = *GP(pold + o);      // p^m
             const float p1 = pc[i + 3];          // p^{m-1}
             float pn, lp;
-            // interior tiles hold no strip cell
-            if (CLS == BWD_INTERIOR || (iz >= NSTRIP && iz < g.nz - NSTRIP && ix >= NSTRIP && ix < g.nx - NSTRIP)) {
+            const bool strip = (GZ && (iz < NSTRIP || iz >= g.nz - NSTRIP)) || (GX && (ix < NSTRIP || ix >= g.nx - NSTRIP));
+            if (!strip) {
                 const int u0 = (r0l + i) * UWP + 1 + cl;        // su index of u position c
                 const float vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
                 const float ux = cf.c0x * (sm.su[SIDX(u0 + 1, NU)] - sm.su[SIDX(u0, NU)]) +
@@ -869,6 +901,164 @@ __global__ void __launch_bounds__(NTH) k_backward(const StepParams P)
             }
             *GP(pold + o) = pn;
             *GP(gacc + o) = fmaf(bm[h * R + i], lp, *GP(gacc + o));
+        }
+    }
+}
+
+// Shared memory of an interior backward tile: the adjoint x stage needs no
+// psi-adjusted copy (srx), so interior blocks are launched with this smaller
+// layout (sizeof(BwdIntSmem) dynamic bytes).
+struct BwdIntSmem {
+    float sq[SPH * SPW];   // b^{m+1} tile + halo
+    float sp[SPH * SPW];   // p^{m-1} tile + halo
+    float su[TZ * UWP];    // adjoint ubar, then rebuild u
+    float racc[TZ * TX];   // receiver adjoint sources of the tile
+};
+
+// Backward step, interior tiles (the rectangle fast_tx0.. x fast_tz0..):
+// every cell and stencil neighbour is a physical interior cell (no CPML,
+// edge formula or strip), so the adjoint is L^T b = the staggered
+// differences with their signs exchanged, the rebuild is the interior
+// operator, and the imaging term is the rebuild's own stencil value.  The
+// per-cell operands (b^{m+2}, K, then p^m and g) are loaded before the
+// shared-memory phases that need them, so their latency overlaps the tile
+// staging and the x stages.
+__global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
+{
+    FWI_DYN_SMEM(smraw);
+    BwdIntSmem& sm = *reinterpret_cast<BwdIntSmem*>(smraw);
+    const Geo& g = P.g;
+    const Coef& cf = P.c;
+    const int s = blockIdx.z + P.shot_base;
+    const ShotDev sd = *GP(P.shots + s);
+    const int m = P.step;
+    if (m > sd.nt) return;
+    const int txi = P.fast_tx0 + blockIdx.x, tzi = P.fast_tz0 + blockIdx.y;
+    const int x0 = txi * TX, z0 = tzi * TZ;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
+    const long long so = (long long)s * g.fstride;
+    float* __restrict__ bold = P.bold + so;
+    float* __restrict__ pold = P.pold + so;
+    float* __restrict__ gacc = P.gacc + so;
+    const int r0l = R * ty, r0 = z0 + r0l;
+    [[maybe_unused]] constexpr int NS = SPH * SPW, NU = TZ * UWP;
+
+    float bo[CX * R], kk[CX * R];
+    #pragma unroll
+    for (int h = 0; h < CX; ++h)
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const long long o = (long long)(r0 + i) * g.ld + x0 + tx + BX * h;
+            bo[h * R + i] = __ldcg(GP(bold + o));
+            kk[h * R + i] = __ldg(GP(P.K + o));
+        }
+    stage_tile(P.bcur + so, g, x0, z0, sm.sq);
+    stage_tile(P.pcur + so, g, x0, z0, sm.sp);
+
+    // adjoint sources r^m at the receivers when m-1 = k*jump
+    const int tile = tzi * g.ntx + txi;
+    const int rb = *GP(P.rtile + sd.rtile_off + tile), re = *GP(P.rtile + sd.rtile_off + tile + 1);
+    const bool do_res = re > rb && ((m - 1) % P.jump) == 0;
+    if (do_res) {
+        for (int q = tid; q < TZ * TX; q += NTH) sm.racc[SIDX(q, TZ * TX)] = 0.f;
+        __syncthreads();
+        const int k = (m - 1) / P.jump;
+        for (int q = rb + tid; q < re; q += NTH) {
+            const RecDev rd = *GP(P.recs + q);
+            atomicAdd(&sm.racc[SIDX(rd.cell, TZ * TX)], *GP(P.res + rd.syn_base + k));
+        }
+    }
+    __syncthreads();
+
+    // adjoint, x: ubar[j] = c0 (q[j-1] - q[j]) + c1 (q[j-2] - q[j+1]) at u positions j in [x0-1, x0+TX+1]
+    #pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int rl = ty + BY * k;
+        #pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            const int jj = tx + BX * h;
+            if (jj >= UW) break;
+            const int q0 = (rl + HZ) * SPW + HX - 1 + jj;         // sq index of column j = x0 - 1 + jj
+            sm.su[SIDX(rl * UWP + jj, NU)] = cf.c0x * (sm.sq[SIDX(q0 - 1, NS)] - sm.sq[SIDX(q0, NS)]) +
+                                             cf.c1x * (sm.sq[SIDX(q0 - 2, NS)] - sm.sq[SIDX(q0 + 1, NS)]);
+        }
+    }
+    __syncthreads();
+
+    // adjoint, z chain in registers, and b^m = 2 b^{m+1} - b^{m+2} + K (L^T b^{m+1} + r^m)
+    float bm[CX * R];
+    #pragma unroll
+    for (int h = 0; h < CX; ++h) {
+        const int cl = tx + BX * h, c = x0 + cl;
+        float qc[R + 6];
+        #pragma unroll
+        for (int k = 0; k < R + 6; ++k) qc[k] = sm.sq[SIDX((r0l + k) * SPW + HX + cl, NS)];   // rows r0-3+k
+        float vb[R + 3];
+        #pragma unroll
+        for (int k = 0; k < R + 3; ++k) vb[k] = cf.c0z * (qc[k + 1] - qc[k + 2]) + cf.c1z * (qc[k] - qc[k + 3]);
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int u0 = (r0l + i) * UWP + 1 + cl;                  // su index of u position c
+            const float pz = cf.c0z * (vb[i + 1] - vb[i + 2]) + cf.c1z * (vb[i] - vb[i + 3]);
+            const float px = cf.c0x * (sm.su[SIDX(u0, NU)] - sm.su[SIDX(u0 + 1, NU)]) +
+                             cf.c1x * (sm.su[SIDX(u0 - 1, NU)] - sm.su[SIDX(u0 + 2, NU)]);
+            float pbar = px + pz;
+            if (do_res) pbar += sm.racc[SIDX((r0l + i) * TX + cl, TZ * TX)];
+            const int q = h * R + i;
+            bm[q] = fmaf(kk[q], pbar, fmaf(2.f, qc[i + 3], -bo[q]));
+            __stcg(GP(bold + (long long)(r0 + i) * g.ld + c), bm[q]);
+        }
+    }
+
+    // rebuild operands, then the rebuild x stage into su (after every thread is done with ubar)
+    float pm[CX * R], ga[CX * R];
+    #pragma unroll
+    for (int h = 0; h < CX; ++h)
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const long long o = (long long)(r0 + i) * g.ld + x0 + tx + BX * h;
+            pm[h * R + i] = __ldcg(GP(pold + o));
+            ga[h * R + i] = __ldcg(GP(gacc + o));
+        }
+    __syncthreads();
+    #pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int rl = ty + BY * k;
+        #pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            const int jj = tx + BX * h;
+            if (jj >= UW) break;
+            const int p0 = (rl + HZ) * SPW + HX - 1 + jj;             // sp index of column j = x0 - 1 + jj
+            sm.su[SIDX(rl * UWP + jj, NU)] = cf.c0x * (sm.sp[SIDX(p0, NS)] - sm.sp[SIDX(p0 - 1, NS)]) +
+                                             cf.c1x * (sm.sp[SIDX(p0 + 1, NS)] - sm.sp[SIDX(p0 - 2, NS)]);
+        }
+    }
+    __syncthreads();
+
+    // rebuild p^{m-2} = 2 p^{m-1} - p^m + K (L p^{m-1} + s^{m-1}) and imaging g += b^m (L p^{m-1} + f^{m-1})
+    const float f = *GP(P.wav + sd.wav_off + m - 1) * cf.iarea;
+    #pragma unroll
+    for (int h = 0; h < CX; ++h) {
+        const int cl = tx + BX * h, c = x0 + cl;
+        float pc[R + 6];
+        #pragma unroll
+        for (int k = 0; k < R + 6; ++k) pc[k] = sm.sp[SIDX((r0l + k) * SPW + HX + cl, NS)];
+        float vv[R + 3];
+        #pragma unroll
+        for (int k = 0; k < R + 3; ++k) vv[k] = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int row = r0 + i, q = h * R + i;
+            const long long o = (long long)row * g.ld + c;
+            const int u0 = (r0l + i) * UWP + 1 + cl;
+            const float vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
+            const float ux = cf.c0x * (sm.su[SIDX(u0 + 1, NU)] - sm.su[SIDX(u0, NU)]) +
+                             cf.c1x * (sm.su[SIDX(u0 + 2, NU)] - sm.su[SIDX(u0 - 1, NU)]);
+            float lp = ux + vz;
+            float pn = fmaf(kk[q], lp, fmaf(2.f, pc[i + 3], -pm[q]));
+            if (row == sd.src_r && c == sd.src_c) { pn += f * kk[q]; lp += f; }
+            __stcg(GP(pold + o), pn);
+            __stcg(GP(gacc + o), fmaf(bm[q], lp, ga[q]));
         }
     }
 }

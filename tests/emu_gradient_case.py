@@ -17,9 +17,9 @@ import oracle as O                         # noqa: E402
 from test_gpu_parity import Case, rel      # noqa: E402
 
 
-def main(fs, nt):
+def main(fs, nt, nx=150, nz=90):
     o64 = O.Oracle("f64")
-    case = Case(O, fs, seed=11 + fs, nt=nt)
+    case = Case(O, fs, seed=11 + fs, nt=nt, nx=nx, nz=nz)
     case.vtrue = (case.vel * 1.03).astype(np.float32)    # signal in the direct waves of a short record
     obs = case.oracle_obs(o64)
     e = case.engine()
@@ -38,4 +38,4 @@ def main(fs, nt):
 
 
 if __name__ == "__main__":
-    main(int(sys.argv[1]), int(sys.argv[2]))
+    main(*[int(a) for a in sys.argv[1:]])

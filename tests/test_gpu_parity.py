@@ -100,10 +100,12 @@ def test_forward_seismograms(lib, oracles, fs):
         assert rel(got, want) <= SYN_TOL, rel(got, want)
 
 
-@pytest.mark.parametrize("fs", [1, 0])
-def test_gradient_against_fp64_oracle(lib, oracles, fs):
+# 150 x 90: full-width edge tiles; 130 x 70: a last tile column under half a
+# tile wide and a last tile row of a few rows (partial general tiles).
+@pytest.mark.parametrize("fs,nx,nz", [(1, 150, 90), (0, 150, 90), (1, 130, 70), (0, 130, 70)])
+def test_gradient_against_fp64_oracle(lib, oracles, fs, nx, nz):
     O, o32, o64 = oracles
-    case = Case(O, fs, seed=3 + fs)
+    case = Case(O, fs, seed=3 + fs, nx=nx, nz=nz)
     obs = case.oracle_obs(o64)
     e = case.engine()
     e.set_model(case.vel)
