@@ -20,7 +20,7 @@ from test_gpu_parity import Case, rel      # noqa: E402
 def main(fs, nt, nx=150, nz=90):
     o64 = O.Oracle("f64")
     case = Case(O, fs, seed=11 + fs, nt=nt, nx=nx, nz=nz)
-    case.vtrue = (case.vel * 1.03).astype(np.float32)    # signal in the direct waves of a short record
+    case.vtrue = (case.vel * 1.08).astype(np.float32)    # signal in the direct waves of a short record
     obs = case.oracle_obs(o64)
     e = case.engine()
     e.set_model(case.vel)
