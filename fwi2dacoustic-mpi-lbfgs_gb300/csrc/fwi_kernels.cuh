@@ -203,16 +203,67 @@ struct StepParams {
 // grid edge (edge and one-sided formulas), a CPML layer (psi recursions) or
 // the boundary strips.  The test separates into x and z, so the interior
 // tiles form a rectangle.
-__host__ __device__ inline bool tile_x_general(const Geo& g, int x0)
+//
+// The same tests apply to any window of w columns (h rows): a window whose
+// test is false lies, with the stencil reach of its outputs (3 cells), inside
+// the region where every formula is the plain interior one.  Inside a
+// general tile, warps use them to take the plain formulas for their own rows
+// (z window of R rows) or column half (x window of BX columns).
+__host__ __device__ inline bool x_window_general(const Geo& g, int x0, int w)
 {
     const int np = g.npml;
-    return x0 < 8 || x0 + TX + 8 > g.pnx || x0 - 4 <= np || x0 + TX + 4 >= g.pnx - np;
+    return x0 < 8 || x0 + w + 8 > g.pnx || x0 - 4 <= np || x0 + w + 4 >= g.pnx - np;
 }
-__host__ __device__ inline bool tile_z_general(const Geo& g, int z0)
+__host__ __device__ inline bool z_window_general(const Geo& g, int z0, int h)
 {
     const int np = g.npml;
-    return z0 < 8 || z0 + TZ + 8 > g.pnz || z0 + TZ + 4 >= g.pnz - np || (!g.fs && z0 - 4 <= np);
+    return z0 < 8 || z0 + h + 8 > g.pnz || z0 + h + 4 >= g.pnz - np || (!g.fs && z0 - 4 <= np);
 }
+__host__ __device__ inline bool tile_x_general(const Geo& g, int x0) { return x_window_general(g, x0, TX); }
+__host__ __device__ inline bool tile_z_general(const Geo& g, int z0) { return z_window_general(g, z0, TZ); }
+
+// CPML psi sites.  Each returns the offset of the psi entry within one shot's
+// psi block (or -1 where the position has none) and the profile node and
+// side of its coefficients (side 0: a0/b0 = left/top, 1: a1/b1 = right/bottom).
+// u positions j in [0, pnx] (fwi_2d.c:790-794), ux cells i in [0, pnx)
+// (838-842), v positions kv in [0, pnz] (816-817; v0 mirrors v1 on top when
+// free_surface == 0), vz cells (860-861).  The kernels read all psi entries
+// of a phase with independent loads before they use any of them.
+struct PsiSite {
+    int idx, node, side;
+};
+__device__ __forceinline__ PsiSite psi_u(const StepParams& P, int row, int j)
+{
+    const int np = P.g.npml, pnx = P.g.pnx;
+    if (j >= 0 && j <= np) return {P.pl.u0 + row * (np + 1) + j, 2 * j, 0};
+    if (j >= pnx - np && j <= pnx) return {P.pl.u1 + row * (np + 1) + (j - (pnx - np)), 2 * (j - (pnx - np)), 1};
+    return {-1, 0, 0};
+}
+__device__ __forceinline__ PsiSite psi_ux(const StepParams& P, int row, int i)
+{
+    const int np = P.g.npml, pnx = P.g.pnx;
+    if (i >= 0 && i < np) return {P.pl.ux0 + row * np + i, 2 * i + 1, 0};
+    if (i >= pnx - np && i < pnx) return {P.pl.ux1 + row * np + (i - (pnx - np)), 2 * (i - (pnx - np)) + 1, 1};
+    return {-1, 0, 0};
+}
+__device__ __forceinline__ PsiSite psi_v(const StepParams& P, int kv, int c)
+{
+    const int np = P.g.npml, pnx = P.g.pnx, pnz = P.g.pnz;
+    if (c < 0 || c >= pnx || kv < 0 || kv > pnz) return {-1, 0, 0};
+    if (kv >= pnz - np) return {P.pl.v1 + (kv - (pnz - np)) * pnx + c, 2 * (kv - (pnz - np)), 1};
+    if (!P.g.fs && kv <= np) return {P.pl.v0 + kv * pnx + c, 2 * kv, 0};
+    return {-1, 0, 0};
+}
+__device__ __forceinline__ PsiSite psi_vz(const StepParams& P, int row, int c)
+{
+    const int np = P.g.npml, pnx = P.g.pnx, pnz = P.g.pnz;
+    if (c < 0 || c >= pnx || row < 0 || row >= pnz) return {-1, 0, 0};
+    if (row >= pnz - np) return {P.pl.vz1 + (row - (pnz - np)) * pnx + c, 2 * (row - (pnz - np)) + 1, 1};
+    if (!P.g.fs && row < np) return {P.pl.vz0 + row * pnx + c, 2 * row + 1, 0};
+    return {-1, 0, 0};
+}
+// psi value of a site (0 where there is none)
+__device__ __forceinline__ float psi_load(const float* psr, const PsiSite& t) { return t.idx >= 0 ? __ldcg(GP(psr + t.idx)) : 0.f; }
 
 // u = staggered d/dx of p at u-position j (fwi_2d.c:775-784); p[row][col]
 // is sp[base + col] (base = row offset - x0 + HX, an integer, so no pointer
@@ -280,7 +331,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
     const Geo& g = P.g;
     const Coef& cf = P.c;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int np = g.npml, n2 = 2 * np + 1;
+    const int n2 = 2 * g.npml + 1;
     const long long so = (long long)s * g.fstride;
     const float* __restrict__ psr = P.psr + (long long)s * P.pl.stride;
     float* __restrict__ psw = P.psw + (long long)s * P.pl.stride;
@@ -289,7 +340,21 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
     const float* a0z = a0x + 4 * n2;    const float* b0z = a0x + 5 * n2;
     const float* a1z = a0x + 6 * n2;    const float* b1z = a0x + 7 * n2;
 
-    // u at positions j in [x0-1, x0+TX+1], rows [z0, z0+TZ)
+    // u at positions j in [x0-1, x0+TX+1], rows [z0, z0+TZ); the psi entries
+    // of the x-general column halves are read first
+    float pu[R][3];
+    if (GX) {
+        #pragma unroll
+        for (int k = 0; k < R; ++k) {
+            const int row = z0 + ty + BY * k;
+            #pragma unroll
+            for (int h = 0; h < 3; ++h) {
+                const int jj = tx + BX * h;
+                const bool gen = jj < UW && !(GZ && row >= g.pnz) && x_window_general(g, x0 - 1 + BX * h, BX);
+                pu[k][h] = gen ? psi_load(psr, psi_u(P, row, x0 - 1 + jj)) : 0.f;
+            }
+        }
+    }
     #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int rl = ty + BY * k, row = z0 + rl;
@@ -301,23 +366,18 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             if (jj >= UW) break;
             const int j = x0 - 1 + jj;
             float u;
-            if (!GX) {
+            if (!GX || !x_window_general(g, x0 - 1 + BX * h, BX)) {        // plain u for this column half
                 const int q = pbase + j;
                 u = cf.c0x * (sp[SIDX(q, SPH * SPW)] - sp[SIDX(q - 1, SPH * SPW)]) +
                     cf.c1x * (sp[SIDX(q + 1, SPH * SPW)] - sp[SIDX(q - 2, SPH * SPW)]);
             } else {
                 u = u_edge(sp, pbase, j, g.pnx, cf);
-                const bool own = jj >= 1 && jj <= TX;
-                if (j >= 0 && j <= np) {                                   // fwi_2d.c:790-791
-                    const int idx = P.pl.u0 + row * (np + 1) + j;
-                    const float ps = *GP(b0x + 2 * j) * *GP(psr + idx) + *GP(a0x + 2 * j) * u;
-                    if (own) *GP(psw + idx) = ps;
-                    u += ps;
-                } else if (j >= g.pnx - np && j <= g.pnx) {               // fwi_2d.c:793-794
-                    const int kk = j - (g.pnx - np);
-                    const int idx = P.pl.u1 + row * (np + 1) + kk;
-                    const float ps = *GP(b1x + 2 * kk) * *GP(psr + idx) + *GP(a1x + 2 * kk) * u;
-                    if (own) *GP(psw + idx) = ps;
+                const PsiSite t = psi_u(P, row, j);                        // fwi_2d.c:790-794
+                if (t.idx >= 0) {
+                    const float* ca = t.side ? a1x : a0x;
+                    const float* cb = t.side ? b1x : b0x;
+                    const float ps = *GP(cb + t.node) * pu[k][h] + *GP(ca + t.node) * u;
+                    if (jj >= 1 && jj <= TX) *GP(psw + t.idx) = ps;
                     u += ps;
                 }
             }
@@ -328,13 +388,30 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
 
     const int r0l = R * ty, r0 = z0 + r0l;
     if (GZ && r0 >= g.pnz) return;                                         // the last phase: no barrier follows
+    const bool gzw = GZ && z_window_general(g, r0, R);                     // this warp's rows need the z-general formulas
     const float* __restrict__ K = P.K;
     float* __restrict__ pold = P.pold + so;
     const float amp = *GP(P.wav + sd.wav_off + P.step) * cf.iarea;
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
         if (GX && x0 + BX * h >= g.pnx) continue;                          // column half past the grid
+        const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);        // this half needs the x-general formulas
         const int cl = tx + BX * h, c = x0 + cl;
+        // every global operand of this column segment first: K, p^{it-1} and the psi entries
+        float kq[R], po[R], pvv[R + 3], pux[R], pvz[R];
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int row = r0 + i;
+            const bool inside = (!GZ || row < g.pnz) && (!GX || c < g.pnx);
+            const long long o = (long long)row * g.ld + c;
+            kq[i] = inside ? __ldg(GP(K + o)) : 0.f;
+            po[i] = inside ? *GP(pold + o) : 0.f;
+            pux[i] = (gxc && inside) ? psi_load(psr, psi_ux(P, row, c)) : 0.f;
+            pvz[i] = (gzw && inside) ? psi_load(psr, psi_vz(P, row, c)) : 0.f;
+        }
+        #pragma unroll
+        for (int k = 0; k < R + 3; ++k) pvv[k] = gzw ? psi_load(psr, psi_v(P, r0 - 1 + k, c)) : 0.f;
+
         float pc[R + 6];
         #pragma unroll
         for (int k = 0; k < R + 6; ++k) pc[k] = sp[SIDX((r0l + k) * SPW + HX + cl, SPH * SPW)];   // rows r0-3+k
@@ -343,7 +420,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
         for (int k = 0; k < R + 3; ++k) {
             const int kv = r0 - 1 + k;
             float v;
-            if (!GZ) {
+            if (!gzw) {
                 v = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
             } else {
                 if (kv >= 2 && kv <= g.pnz - 2) {
@@ -358,20 +435,13 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                 } else {
                     v = 0.f;
                 }
-                if ((!GX || c < g.pnx) && kv >= 0 && kv <= g.pnz) {
-                    const bool own = k >= 1 && k <= R && kv < g.pnz;
-                    if (kv >= g.pnz - np) {                               // fwi_2d.c:816-817
-                        const int kk = kv - (g.pnz - np);
-                        const int idx = P.pl.v1 + kk * g.pnx + c;
-                        const float ps = *GP(b1z + 2 * kk) * *GP(psr + idx) + *GP(a1z + 2 * kk) * v;
-                        if (own) *GP(psw + idx) = ps;
-                        v += ps;
-                    } else if (!g.fs && kv <= np) {                       // top layer, all-sides CPML
-                        const int idx = P.pl.v0 + kv * g.pnx + c;
-                        const float ps = *GP(b0z + 2 * kv) * *GP(psr + idx) + *GP(a0z + 2 * kv) * v;
-                        if (own) *GP(psw + idx) = ps;
-                        v += ps;
-                    }
+                const PsiSite t = psi_v(P, kv, c);                        // fwi_2d.c:816-817 (v0: top, all sides)
+                if (t.idx >= 0) {
+                    const float* ca = t.side ? a1z : a0z;
+                    const float* cb = t.side ? b1z : b0z;
+                    const float ps = *GP(cb + t.node) * pvv[k] + *GP(ca + t.node) * v;
+                    if (k >= 1 && k <= R && kv < g.pnz) *GP(psw + t.idx) = ps;
+                    v += ps;
                 }
             }
             vv[k] = v;
@@ -382,7 +452,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             const int ubase = (r0l + i) * UWP + 1 - x0;                     // + u position = su index
             #define UR(j) su[SIDX(ubase + (j), TZ * UWP)]
             float vz, ux;
-            if (!GZ) {
+            if (!gzw) {
                 vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
             } else {
                 if (row >= 1 && row <= g.pnz - 2) {
@@ -400,7 +470,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                     vz = 0.f;
                 }
             }
-            if (!GX) {
+            if (!gxc) {
                 ux = cf.c0x * (UR(c + 1) - UR(c)) + cf.c1x * (UR(c + 2) - UR(c - 1));
             } else {
                 if (c >= 1 && c <= g.pnx - 2) {
@@ -415,41 +485,32 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             }
             #undef UR
             const bool inside = (!GZ || row < g.pnz) && (!GX || c < g.pnx);
-            if (GX && inside) {
-                if (c < np) {                                             // fwi_2d.c:838-839
-                    const int idx = P.pl.ux0 + row * np + c;
-                    const float ps = *GP(b0x + 2 * c + 1) * *GP(psr + idx) + *GP(a0x + 2 * c + 1) * ux;
-                    *GP(psw + idx) = ps;
-                    ux += ps;
-                } else if (c >= g.pnx - np) {                             // fwi_2d.c:841-842
-                    const int kk = c - (g.pnx - np);
-                    const int idx = P.pl.ux1 + row * np + kk;
-                    const float ps = *GP(b1x + 2 * kk + 1) * *GP(psr + idx) + *GP(a1x + 2 * kk + 1) * ux;
-                    *GP(psw + idx) = ps;
+            if (gxc && inside) {
+                const PsiSite t = psi_ux(P, row, c);                      // fwi_2d.c:838-842
+                if (t.idx >= 0) {
+                    const float* ca = t.side ? a1x : a0x;
+                    const float* cb = t.side ? b1x : b0x;
+                    const float ps = *GP(cb + t.node) * pux[i] + *GP(ca + t.node) * ux;
+                    *GP(psw + t.idx) = ps;
                     ux += ps;
                 }
             }
-            if (GZ && inside) {
-                if (row >= g.pnz - np) {                                  // fwi_2d.c:860-861
-                    const int kk = row - (g.pnz - np);
-                    const int idx = P.pl.vz1 + kk * g.pnx + c;
-                    const float ps = *GP(b1z + 2 * kk + 1) * *GP(psr + idx) + *GP(a1z + 2 * kk + 1) * vz;
-                    *GP(psw + idx) = ps;
-                    vz += ps;
-                } else if (!g.fs && row < np) {
-                    const int idx = P.pl.vz0 + row * g.pnx + c;
-                    const float ps = *GP(b0z + 2 * row + 1) * *GP(psr + idx) + *GP(a0z + 2 * row + 1) * vz;
-                    *GP(psw + idx) = ps;
+            if (gzw && inside) {
+                const PsiSite t = psi_vz(P, row, c);                      // fwi_2d.c:860-861
+                if (t.idx >= 0) {
+                    const float* ca = t.side ? a1z : a0z;
+                    const float* cb = t.side ? b1z : b0z;
+                    const float ps = *GP(cb + t.node) * pvz[i] + *GP(ca + t.node) * vz;
+                    *GP(psw + t.idx) = ps;
                     vz += ps;
                 }
             }
             if (inside) {
                 const long long o = (long long)row * g.ld + c;
-                const float kk = __ldg(GP(K + o));
-                float pn = fmaf(kk, ux + vz, fmaf(2.f, pc[i + 3], -*GP(pold + o)));      // fwi_2d.c:878
-                if (row == sd.src_r && c == sd.src_c) pn += amp * kk;
+                float pn = fmaf(kq[i], ux + vz, fmaf(2.f, pc[i + 3], -po[i]));      // fwi_2d.c:878
+                if (row == sd.src_r && c == sd.src_c) pn += amp * kq[i];
                 *GP(pold + o) = pn;
-                save_strip(P, sd, row, c, pn, P.step);
+                if (gzw || gxc) save_strip(P, sd, row, c, pn, P.step);    // plain windows hold no strip cell
             }
         }
     }
@@ -577,7 +638,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     const Geo& g = P.g;
     const Coef& cf = P.c;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int np = g.npml, n2 = 2 * np + 1, pnx = g.pnx, pnz = g.pnz;
+    const int n2 = 2 * g.npml + 1, pnx = g.pnx, pnz = g.pnz;
     const long long so = (long long)s * g.fstride;
     const float* __restrict__ psr = P.psr + (long long)s * P.pl.stride;
     float* __restrict__ psw = P.psw + (long long)s * P.pl.stride;
@@ -586,6 +647,25 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     const float* a0z = a0x + 4 * n2;    const float* b0z = a0x + 5 * n2;
     const float* a1z = a0x + 6 * n2;    const float* b1z = a0x + 7 * n2;
     [[maybe_unused]] constexpr int NS = SPH * SPW, NU = TZ * UWP, NR = TZ * RXP;
+
+    // psi entries of both x stages first (independent loads): the ux
+    // recursion at cells i = x0-3+ii and the u recursion at positions
+    // j = x0-1+jj of the x-general column halves
+    float pux[R][3], pu[R][3];
+    if (GX) {
+        #pragma unroll
+        for (int k = 0; k < R; ++k) {
+            const int row = z0 + ty + BY * k;
+            const bool live = !(GZ && row >= pnz);
+            #pragma unroll
+            for (int h = 0; h < 3; ++h) {
+                const int ii = tx + BX * h, jj = ii;
+                pux[k][h] = (live && ii < RXW) ? psi_load(psr, psi_ux(P, row, x0 - 3 + ii)) : 0.f;
+                const bool gen = live && jj < UW && x_window_general(g, x0 - 1 + BX * h, BX);
+                pu[k][h] = gen ? psi_load(psr, psi_u(P, row, x0 - 1 + jj)) : 0.f;
+            }
+        }
+    }
 
     // x stage 1 (x-general tiles): rbar = q adjusted by the adjoint of the ux psi recursion
     if (GX) {
@@ -598,22 +678,14 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             for (int h = 0; h < 3; ++h) {
                 const int ii = tx + BX * h;
                 if (ii >= RXW) break;
-                const int i = x0 - 3 + ii;
                 float r = sm.sq[SIDX(qrow + ii, NS)];
-                if (i >= 0 && i < pnx) {
-                    const bool own = ii >= 3 && ii < 3 + TX;
-                    if (i < np) {
-                        const int idx = P.pl.ux0 + row * np + i;
-                        const float t = r + *GP(psr + idx);
-                        r = r + *GP(a0x + 2 * i + 1) * t;
-                        if (own) *GP(psw + idx) = *GP(b0x + 2 * i + 1) * t;
-                    } else if (i >= pnx - np) {
-                        const int kk = i - (pnx - np);
-                        const int idx = P.pl.ux1 + row * np + kk;
-                        const float t = r + *GP(psr + idx);
-                        r = r + *GP(a1x + 2 * kk + 1) * t;
-                        if (own) *GP(psw + idx) = *GP(b1x + 2 * kk + 1) * t;
-                    }
+                const PsiSite t = psi_ux(P, row, x0 - 3 + ii);
+                if (t.idx >= 0) {
+                    const float* ca = t.side ? a1x : a0x;
+                    const float* cb = t.side ? b1x : b0x;
+                    const float tt = r + pux[k][h];
+                    r = r + *GP(ca + t.node) * tt;
+                    if (ii >= 3 && ii < 3 + TX) *GP(psw + t.idx) = *GP(cb + t.node) * tt;
                 }
                 sm.srx[SIDX(rl * RXP + ii, NR)] = r;
             }
@@ -631,7 +703,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             if (jj >= UW) break;
             const int j = x0 - 1 + jj;
             float ub;
-            if (!GX) {
+            if (!GX || !x_window_general(g, x0 - 1 + BX * h, BX)) {        // plain ubar for this column half
                 const int q0 = (rl + HZ) * SPW + HX - 1 + jj;     // sq index of column j
                 ub = cf.c0x * (sm.sq[SIDX(q0 - 1, NS)] - sm.sq[SIDX(q0, NS)]) +
                      cf.c1x * (sm.sq[SIDX(q0 - 2, NS)] - sm.sq[SIDX(q0 + 1, NS)]);
@@ -644,18 +716,13 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 if (j == 0) ub -= cf.ix * sm.srx[SIDX(rbase, NR)];
                 if (j == pnx) ub += cf.ix * sm.srx[SIDX(rbase + pnx - 1, NR)];
                 if (j == pnx - 1) ub -= cf.ix * sm.srx[SIDX(rbase + pnx - 1, NR)];
-                const bool own = jj >= 1 && jj <= TX;
-                if (j >= 0 && j <= np) {
-                    const int idx = P.pl.u0 + row * (np + 1) + j;
-                    const float t = ub + *GP(psr + idx);
-                    ub = ub + *GP(a0x + 2 * j) * t;
-                    if (own) *GP(psw + idx) = *GP(b0x + 2 * j) * t;
-                } else if (j >= pnx - np && j <= pnx) {
-                    const int kk = j - (pnx - np);
-                    const int idx = P.pl.u1 + row * (np + 1) + kk;
-                    const float t = ub + *GP(psr + idx);
-                    ub = ub + *GP(a1x + 2 * kk) * t;
-                    if (own) *GP(psw + idx) = *GP(b1x + 2 * kk) * t;
+                const PsiSite t = psi_u(P, row, j);
+                if (t.idx >= 0) {
+                    const float* ca = t.side ? a1x : a0x;
+                    const float* cb = t.side ? b1x : b0x;
+                    const float tt = ub + pu[k][h];
+                    ub = ub + *GP(ca + t.node) * tt;
+                    if (jj >= 1 && jj <= TX) *GP(psw + t.idx) = *GP(cb + t.node) * tt;
                 }
             }
             sm.su[SIDX(rl * UWP + jj, NU)] = ub;
@@ -665,12 +732,29 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
 
     const int r0l = R * ty, r0 = z0 + r0l;
     if (GZ && r0 >= pnz) return;                 // no rows of this thread exist; the caller skips them too
+    const bool gzw = GZ && z_window_general(g, r0, R);                     // this warp's rows need the z-general formulas
     const float* __restrict__ K = P.K;
     float* __restrict__ bold = P.bold + so;
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
         if (GX && x0 + BX * h >= pnx) continue;
+        const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);        // this half needs the x-general formulas
         const int cl = tx + BX * h, c = x0 + cl;
+        // every global operand of this column segment first: K, b^{m+2} and the psi entries
+        float kq[R], bo[R], prz[R + 6], pvb[R + 3];
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int row = r0 + i;
+            const bool inside = (!GZ || row < pnz) && (!GX || c < pnx);
+            const long long o = (long long)row * g.ld + c;
+            kq[i] = inside ? __ldg(GP(K + o)) : 0.f;
+            bo[i] = inside ? *GP(bold + o) : 0.f;
+        }
+        #pragma unroll
+        for (int k = 0; k < R + 6; ++k) prz[k] = gzw ? psi_load(psr, psi_vz(P, r0 - 3 + k, c)) : 0.f;
+        #pragma unroll
+        for (int k = 0; k < R + 3; ++k) pvb[k] = gzw ? psi_load(psr, psi_v(P, r0 - 1 + k, c)) : 0.f;
+
         float qc[R + 6];
         #pragma unroll
         for (int k = 0; k < R + 6; ++k) qc[k] = sm.sq[SIDX((r0l + k) * SPW + HX + cl, NS)];   // rows r0-3+k
@@ -678,22 +762,14 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         #pragma unroll
         for (int k = 0; k < R + 6; ++k) {
             float r = qc[k];
-            if (GZ) {
-                const int row = r0 - 3 + k;
-                if (row >= 0 && row < pnz && (!GX || c < pnx)) {
-                    const bool own = k >= 3 && k < 3 + R;
-                    if (row >= pnz - np) {
-                        const int kk = row - (pnz - np);
-                        const int idx = P.pl.vz1 + kk * pnx + c;
-                        const float t = r + *GP(psr + idx);
-                        r = r + *GP(a1z + 2 * kk + 1) * t;
-                        if (own) *GP(psw + idx) = *GP(b1z + 2 * kk + 1) * t;
-                    } else if (!g.fs && row < np) {
-                        const int idx = P.pl.vz0 + row * pnx + c;
-                        const float t = r + *GP(psr + idx);
-                        r = r + *GP(a0z + 2 * row + 1) * t;
-                        if (own) *GP(psw + idx) = *GP(b0z + 2 * row + 1) * t;
-                    }
+            if (gzw) {
+                const PsiSite t = psi_vz(P, r0 - 3 + k, c);
+                if (t.idx >= 0) {
+                    const float* ca = t.side ? a1z : a0z;
+                    const float* cb = t.side ? b1z : b0z;
+                    const float tt = r + prz[k];
+                    r = r + *GP(ca + t.node) * tt;
+                    if (k >= 3 && k < 3 + R) *GP(psw + t.idx) = *GP(cb + t.node) * tt;
                 }
             }
             rz[k] = r;
@@ -703,7 +779,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         for (int k = 0; k < R + 3; ++k) {
             const int kv = r0 - 1 + k;
             float v;
-            if (!GZ) {
+            if (!gzw) {
                 v = cf.c0z * (rz[k + 1] - rz[k + 2]) + cf.c1z * (rz[k] - rz[k + 3]);
             } else {
                 // rz index of row q is q - (r0 - 3); row kv-1 -> k+1 etc.
@@ -726,20 +802,13 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 }
                 if (kv == pnz) v += cf.iz * rz[k + 1];
                 if (kv == pnz - 1) v -= cf.iz * rz[k + 2];
-                if ((!GX || c < pnx) && kv >= 0 && kv <= pnz) {
-                    const bool own = k >= 1 && k <= R && kv < pnz;
-                    if (kv >= pnz - np) {
-                        const int kk = kv - (pnz - np);
-                        const int idx = P.pl.v1 + kk * pnx + c;
-                        const float t = v + *GP(psr + idx);
-                        v = v + *GP(a1z + 2 * kk) * t;
-                        if (own) *GP(psw + idx) = *GP(b1z + 2 * kk) * t;
-                    } else if (!g.fs && kv <= np) {
-                        const int idx = P.pl.v0 + kv * pnx + c;
-                        const float t = v + *GP(psr + idx);
-                        v = v + *GP(a0z + 2 * kv) * t;
-                        if (own) *GP(psw + idx) = *GP(b0z + 2 * kv) * t;
-                    }
+                const PsiSite t = psi_v(P, kv, c);
+                if (t.idx >= 0) {
+                    const float* ca = t.side ? a1z : a0z;
+                    const float* cb = t.side ? b1z : b0z;
+                    const float tt = v + pvb[k];
+                    v = v + *GP(ca + t.node) * tt;
+                    if (k >= 1 && k <= R && kv < pnz) *GP(psw + t.idx) = *GP(cb + t.node) * tt;
                 }
             }
             vb[k] = v;
@@ -750,7 +819,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             const int ubase = (r0l + i) * UWP + 1 - x0;                   // + u position = su index
             #define UB(j) sm.su[SIDX(ubase + (j), NU)]
             float pz, px;
-            if (!GZ) {
+            if (!gzw) {
                 pz = cf.c0z * (vb[i + 1] - vb[i + 2]) + cf.c1z * (vb[i] - vb[i + 3]);
             } else {
                 // vbar index of row q is q - (r0 - 1)
@@ -772,7 +841,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 if (row == pnz - 1) pz += cf.iz * vb[i + 1];
                 if (row == pnz - 2) pz -= cf.iz * vb[i + 2];
             }
-            if (!GX) {
+            if (!gxc) {
                 px = cf.c0x * (UB(c) - UB(c + 1)) + cf.c1x * (UB(c - 1) - UB(c + 2));
             } else {
                 #define UM(j) (((j) >= 2 && (j) <= pnx - 2) ? UB(j) : 0.f)
@@ -789,7 +858,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             float b = 0.f;
             if ((!GZ || row < pnz) && (!GX || c < pnx)) {
                 const long long o = (long long)row * g.ld + c;
-                b = fmaf(__ldg(GP(K + o)), pbar, fmaf(2.f, qc[i + 3], -*GP(bold + o)));
+                b = fmaf(kq[i], pbar, fmaf(2.f, qc[i + 3], -bo[i]));
                 *GP(bold + o) = b;
             }
             bm[h * R + i] = b;
@@ -860,6 +929,7 @@ __global__ void __launch_bounds__(NTH, 3) k_bwd_edge(const StepParams P)
     __syncthreads();
     const int r0l = R * ty, r0 = z0 + r0l;
     if (GZ && (r0 >= zp1 || r0 + R <= zp0)) return;   // no physical row of this thread; no barrier follows
+    const bool gzw = GZ && z_window_general(g, r0, R);  // rows that may be outside the region or strips
     const float* __restrict__ K = P.K;
     float* __restrict__ pold = P.pold + so;
     float* __restrict__ gacc = P.gacc + so;
@@ -867,9 +937,23 @@ __global__ void __launch_bounds__(NTH, 3) k_bwd_edge(const StepParams P)
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
         if (GX && (x0 + BX * h >= xp1 || x0 + BX * h + BX <= xp0)) continue;   // no physical column in this half
+        const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);
         const int cl = tx + BX * h, c = x0 + cl;
         const int ix = c - g.x0p;
-        if (GX && (ix < 0 || ix >= g.nx)) continue;
+        if (gxc && (ix < 0 || ix >= g.nx)) continue;
+        // every global operand of this column segment first: K, p^m, g and the strip values
+        float kq[R], pmq[R], gq[R], pst[R];
+        #pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int row = r0 + i, iz = row - g.z0p;
+            const bool live = !(gzw && (iz < 0 || iz >= g.nz));
+            const bool strip = (gzw && (iz < NSTRIP || iz >= g.nz - NSTRIP)) || (gxc && (ix < NSTRIP || ix >= g.nx - NSTRIP));
+            const long long o = (long long)row * g.ld + c;
+            kq[i] = live ? __ldg(GP(K + o)) : 1.f;
+            pmq[i] = live ? *GP(pold + o) : 0.f;
+            gq[i] = live ? *GP(gacc + o) : 0.f;
+            pst[i] = (live && strip && m - 3 >= 0) ? load_strip(P, sd, iz, ix, m - 3) : 0.f;
+        }
         float pc[R + 6];
         #pragma unroll
         for (int k = 0; k < R + 6; ++k) pc[k] = sm.sp[SIDX((r0l + k) * SPW + HX + cl, NS)];
@@ -879,13 +963,13 @@ __global__ void __launch_bounds__(NTH, 3) k_bwd_edge(const StepParams P)
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i, iz = row - g.z0p;
-            if (GZ && (iz < 0 || iz >= g.nz)) continue;
+            if (gzw && (iz < 0 || iz >= g.nz)) continue;
             const long long o = (long long)row * g.ld + c;
-            const float kk = __ldg(GP(K + o));
-            const float pm = *GP(pold + o);      // p^m
+            const float kk = kq[i];
+            const float pm = pmq[i];             // p^m
             const float p1 = pc[i + 3];          // p^{m-1}
             float pn, lp;
-            const bool strip = (GZ && (iz < NSTRIP || iz >= g.nz - NSTRIP)) || (GX && (ix < NSTRIP || ix >= g.nx - NSTRIP));
+            const bool strip = (gzw && (iz < NSTRIP || iz >= g.nz - NSTRIP)) || (gxc && (ix < NSTRIP || ix >= g.nx - NSTRIP));
             if (!strip) {
                 const int u0 = (r0l + i) * UWP + 1 + cl;        // su index of u position c
                 const float vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
@@ -896,11 +980,11 @@ __global__ void __launch_bounds__(NTH, 3) k_bwd_edge(const StepParams P)
                 lp = w;
                 if (row == sd.src_r && c == sd.src_c) { pn += f * kk; lp += f; }
             } else {
-                pn = (m - 3 >= 0) ? load_strip(P, sd, iz, ix, m - 3) : 0.f;
+                pn = pst[i];
                 lp = ((pm - 2.f * p1) + pn) / kk;
             }
             *GP(pold + o) = pn;
-            *GP(gacc + o) = fmaf(bm[h * R + i], lp, *GP(gacc + o));
+            *GP(gacc + o) = fmaf(bm[h * R + i], lp, gq[i]);
         }
     }
 }
