@@ -281,3 +281,122 @@ class RefKernels:
         if st:
             raise ValueError(f"ref_forward failed: {st}")
         return syn, pf, pp, fs, rs
+
+
+# ---------------------------------------------------------------------------
+# Routines around the gradient: preconditioning, band-pass, XCORR misfit
+# ---------------------------------------------------------------------------
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class _AuxCalls:
+    """Shared ctypes calls of the aux oracle and the reference's own routines;
+    `pre` is the symbol prefix ("orc_" or "ref_")."""
+
+    def _setup(self, lib, pre):
+        self.lib, self.pre = lib, pre
+        f = getattr(lib, pre + "grad_precond")
+        f.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int,
+                      C.c_float, C.POINTER(C.c_int)]
+        f.restype = C.c_int
+        f = getattr(lib, pre + "triangle2")
+        f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        f.restype = C.c_int
+        f = getattr(lib, pre + "xcorr1d")
+        if pre == "ref_":
+            f.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_float),
+                          C.c_float, C.c_float, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        else:
+            f.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_float),
+                          C.c_float, C.c_float, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        f.restype = C.c_int
+
+    def grad_precond(self, body, perc, rectx1, repeat1, rectx2, repeat2, alpha_grad, bottom):
+        """grad_precond_new5 (grad_prec.c:5-52) of body[mnz][mnx]; returns a new array."""
+        out = _f32(body).copy()
+        mnz, mnx = out.shape
+        bot = np.ascontiguousarray(bottom, dtype=np.int32)
+        assert bot.shape == (mnx,)
+        st = getattr(self.lib, self.pre + "grad_precond")(_ptr(out, C.c_float), mnx, mnz, perc, rectx1, repeat1,
+                                                          rectx2, repeat2, alpha_grad, _ptr(bot, C.c_int))
+        assert st == 0
+        return out
+
+    def triangle2(self, rect1, rect2, nt, uu):
+        uu = _f32(uu)
+        n2, n1 = uu.shape
+        vv = np.zeros_like(uu)
+        assert getattr(self.lib, self.pre + "triangle2")(rect1, rect2, nt, n1, n2, _ptr(uu, C.c_float),
+                                                         _ptr(vv, C.c_float)) == 0
+        return vv
+
+    def xcorr1d(self, obs, syn, sr_xyz, omin, omax, mode, npad=0):
+        """XCORR1D (xcorr_msf.c:4-181) of traces [nr][nt]; mode 0 middle, 1 leading.
+        Returns (misfit[2] float32, res [nr][nt])."""
+        obs, syn, sr = _f32(obs), _f32(syn), _f32(sr_xyz)
+        nr, nt = obs.shape
+        mis = np.zeros(2, np.float32)
+        res = np.zeros_like(obs)
+        f = getattr(self.lib, self.pre + "xcorr1d")
+        if self.pre == "ref_":
+            st = f(_ptr(obs, C.c_float), _ptr(syn, C.c_float), nr, nt, _ptr(sr, C.c_float), omin, omax, npad, mode,
+                   _ptr(mis, C.c_float), _ptr(res, C.c_float))
+        else:
+            st = f(_ptr(obs, C.c_float), _ptr(syn, C.c_float), nr, nt, _ptr(sr, C.c_float), omin, omax, mode,
+                   _ptr(mis, C.c_float), _ptr(res, C.c_float))
+        assert st == 0
+        return mis, res
+
+
+class AuxOracle(_AuxCalls):
+    """The CPU restatement (fwi_oracle_aux.c) of grad_precond_new5, triangle2,
+    sfbandpass and XCORR1D."""
+
+    def __init__(self):
+        lib = C.CDLL(os.path.join(BUILD, "libfwioracle_aux.so"))
+        self._setup(lib, "orc_")
+        lib.orc_bandpass.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int,
+                                     C.c_float, C.c_float, C.POINTER(C.c_float)]
+        lib.orc_bandpass.restype = C.c_int
+        lib.orc_butter_init.argtypes = [C.c_int, C.c_float, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        lib.orc_butter_init.restype = None
+
+    def bandpass(self, traces, dt, phase, nphi, nplo, fhi, flo):
+        """sfbandpass (butterworth_filter.c:127-200) of traces [nr][nt]."""
+        x = _f32(traces)
+        nr, nt = x.shape
+        out = np.zeros_like(x)
+        st = self.lib.orc_bandpass(_ptr(x, C.c_float), nt, nr, dt, int(phase), nphi, nplo, fhi, flo,
+                                   _ptr(out, C.c_float))
+        assert st == 0, st
+        return out
+
+    def butter_init(self, low, cutoff, nn):
+        den = np.zeros(2 * ((nn + 1) // 2) + 2, np.float32)
+        mid = C.c_float()
+        self.lib.orc_butter_init(int(low), cutoff, nn, _ptr(den, C.c_float), C.byref(mid))
+        return den[:2 * ((nn + 1) // 2)], mid.value
+
+
+class RefAux(_AuxCalls):
+    """The reference's own grad_precond_new5 / triangle2 / sfbandpass / XCORR1D
+    from ``make ref`` (only where the reference sources are available)."""
+
+    @classmethod
+    def available(cls) -> bool:
+        return os.path.isfile(os.path.join(REFDIR, "libfwiref.so"))
+
+    def __init__(self):
+        lib = C.CDLL(os.path.join(REFDIR, "libfwiref.so"))
+        self._setup(lib, "ref_")
+        lib.sfbandpass.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.c_float, C.c_bool, C.c_int, C.c_int,
+                                   C.c_float, C.c_float, C.POINTER(C.c_float)]
+        lib.sfbandpass.restype = None
+
+    def bandpass(self, traces, dt, phase, nphi, nplo, fhi, flo):
+        x = _f32(traces).copy()
+        nr, nt = x.shape
+        out = np.zeros_like(x)
+        self.lib.sfbandpass(_ptr(x, C.c_float), nt, nr, dt, bool(phase), nphi, nplo, fhi, flo, _ptr(out, C.c_float))
+        return out

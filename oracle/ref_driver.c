@@ -257,3 +257,36 @@ int ref_forward(const orc_config *cfg, const float *vel, const orc_shot *sh, int
     free2d(ekp); free(vm); state_free(&fw); plan_free(p);
     return 0;
 }
+
+/* ---- routines around the gradient ---------------------------------------
+ * grad_precond_new5  grad_prec.c:5-52 (with triangle2, triangle_smooth.c:70-110,
+ *                    and argmin/argmax, min_max.c)
+ * sfbandpass         butterworth_filter.c:127-200 (exported as is)
+ * XCORR1D            xcorr_msf.c:4-181 (FFTW/CBLAS from ref_fftw_shim.c)
+ */
+int ref_grad_precond(float *body, int mnx, int mnz, float perc, int rectx1, int repeat1,
+                     int rectx2, int repeat2, float alpha_grad, int *bottom)
+{
+    fwi_grad g = {0, 0.f, 0.f, alpha_grad, perc, 1, (size_t)rectx1, (size_t)rectx1, (size_t)repeat1,
+                  (size_t)rectx2, (size_t)rectx2, (size_t)repeat2, body};
+    fwi_shape bw = {(size_t)mnx, (size_t)mnz, 0, 0, 0, 0, 0, 0};
+    grad_precond_new5(&g, &bw, bottom);
+    return 0;
+}
+
+int ref_triangle2(int rect1, int rect2, int nt, int n1, int n2, float *uu, float *vv)
+{
+    triangle2(rect1, rect2, nt, n1, n2, uu, vv);
+    return 0;
+}
+
+int ref_xcorr1d(const float *obs, const float *syn, int nr, int nt, float *sr_xyz, float omin, float omax,
+                int npad, int mode, float *misfit, float *res)
+{
+    float **o = rows_of((float *)obs, nt, nr), **s = rows_of((float *)syn, nt, nr), **r = rows_of(res, nt, nr);
+    char slice_middle[] = "middle", slice_leading[] = "leading";
+    par_xcorr1d par = {nr, nt, npad, mode == 0 ? slice_middle : slice_leading};
+    XCORR1D(o, s, sr_xyz, omin, omax, &par, misfit, r);
+    free(o); free(s); free(r);
+    return 0;
+}

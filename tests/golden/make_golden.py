@@ -10,7 +10,9 @@ model_ext_fs_no, a_lap_opt_2d_pml (one step, with psi), a_lap_opt_2d,
 write_bdr / write_bdr_fs_no, and a full forward + boundary-strip rebuild
 (a_lap_opt_2d_pml + time_integral forward, read_bdr + a_lap_opt_2d +
 time_integral backward, chunked through a temporary file) on a small free-surface
-case.  The inputs are regenerated from the seeds stored alongside.
+case, and ``tests/golden/ref_aux.npz``: outputs of grad_precond_new5,
+sfbandpass and XCORR1D (``--aux`` writes only this file).  The inputs are
+regenerated from the seeds stored alongside.
 """
 from __future__ import annotations
 
@@ -50,6 +52,65 @@ def case_inputs():
     return cfg, vel, shot, p_fs, p_nofs, p_int, model, steps
 
 
+# (perc, rectx1, repeat1, rectx2, repeat2, alpha_grad) of the preconditioning cases
+PRECOND_CASES = [(0.9, 5, 2, 3, 1, 1.5), (0.0, 1, 1, 7, 3, 2.0), (0.5, 11, 1, 2, 2, 0.3)]
+# (dt, phase, nphi, nplo, fhi, flo) of the band-pass cases: zero-phase and
+# minimum-phase, odd and even orders, low-cut only, high-cut only
+BANDPASS_CASES = [(0.002, 0, 6, 6, 30.0, 3.0), (0.001, 1, 5, 3, 60.0, 5.0), (0.004, 0, 4, 4, 40.0, 0.0),
+                  (0.004, 1, 1, 2, 200.0, 10.0)]
+# (mode, offset min, offset max, traces) of the XCORR cases; mode 0 "middle",
+# 1 "leading"; traces "pulse" (wavelets with lags of both signs) or "noise"
+# (broadband traces that correlate at every lag: in "leading" mode the kept
+# residual window holds no correlation peak of pulse-like traces)
+XCORR_CASES = [(0, 50.0, 550.0, "pulse"), (1, 0.0, 1.0e9, "noise"), (0, 0.0, 1.0e9, "noise")]
+
+
+def aux_inputs():
+    """Deterministic inputs of the preconditioning, band-pass and XCORR cases."""
+    rng = np.random.default_rng(SEED + 7)
+    grad = rng.standard_normal((37, 53)).astype(np.float32)
+    bottom = rng.integers(0, 6, 53).astype(np.int32)
+    traces = rng.standard_normal((9, 400)).astype(np.float32)
+    nt, nr = 121, 7
+    t = np.arange(nt)
+    # obs and syn wavelets with lags of both signs, one trace 20x weaker
+    # (skipped by the energy test) and offsets 0..600 m (two outside [50, 550])
+    obs = np.stack([np.exp(-((t - 60 - 3 * i) / 6.0) ** 2) * np.cos(0.3 * (t - 60)) for i in range(nr)])
+    syn = np.stack([1.2 * np.exp(-((t - 60 + 4 * (i - 3)) / 6.0) ** 2) * np.cos(0.3 * (t - 57)) for i in range(nr)])
+    syn[5] *= 0.04
+    obs, syn = obs.astype(np.float32), syn.astype(np.float32)
+    sr = np.array([0.0, 0.0] + sum([[100.0 * i, 2.0] for i in range(nr)], []), np.float32)
+    return grad, bottom, traces, obs, syn, sr
+
+
+def xcorr_traces(kind):
+    """(obs, syn, sr_xyz) of an XCORR case."""
+    *_, obs, syn, sr = aux_inputs()
+    if kind == "noise":
+        rng = np.random.default_rng(SEED + 8)
+        obs = rng.standard_normal(obs.shape).astype(np.float32)
+        syn = (np.roll(obs, 2, axis=1) + 0.3 * rng.standard_normal(obs.shape)).astype(np.float32)
+    return obs, syn, sr
+
+
+def main_aux() -> None:
+    if not O.RefAux.available():
+        raise SystemExit("reference routines not built")
+    ref = O.RefAux()
+    grad, bottom, traces, obs, syn, sr = aux_inputs()
+    out = {}
+    for k, c in enumerate(PRECOND_CASES):
+        out[f"precond_{k}"] = ref.grad_precond(grad, *c, bottom)
+    for k, c in enumerate(BANDPASS_CASES):
+        out[f"bandpass_{k}"] = ref.bandpass(traces, *c)
+    for k, (mode, omin, omax, kind) in enumerate(XCORR_CASES):
+        o, sy, s_r = xcorr_traces(kind)
+        out[f"xcorr_mis_{k}"], out[f"xcorr_res_{k}"] = ref.xcorr1d(o, sy, s_r, omin, omax, mode, npad=5)
+    path = os.path.join(HERE, "ref_aux.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 def main(ref_dir: str) -> None:
     O.build(ref_dir, quiet=False)
     if not O.RefKernels.available():
@@ -80,5 +141,8 @@ def main(ref_dir: str) -> None:
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--aux" in sys.argv:
+    O.build(next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference"), quiet=False)
+    main_aux()
+elif __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
