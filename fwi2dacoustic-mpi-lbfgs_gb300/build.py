@@ -2,7 +2,8 @@
 
     python fwi2dacoustic-mpi-lbfgs_gb300/build.py [--force]
 
-Compiles ``csrc/fwi_engine.cu`` (which includes ``csrc/fwi_kernels.cuh``) with
+Compiles ``csrc/fwi_engine.cu`` (which includes ``csrc/fwi_kernels.cuh``) and
+``csrc/fwi_aux.cu`` (``csrc/fwi_aux.cuh``) with
 nvcc for ``-gencode arch=compute_103a,code=sm_103a`` into
 ``libfwigpu.so`` next to this file.  The CUDA runtime is linked statically so
 the library only needs the driver at run time.
@@ -17,8 +18,9 @@ import sys
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 LIB = os.path.join(PKG, "libfwigpu.so")
-SOURCES = [os.path.join(PKG, "csrc", "fwi_engine.cu")]
-DEPS = SOURCES + [os.path.join(PKG, "csrc", "fwi_kernels.cuh"), os.path.join(ROOT, "include", "fwi_gb300.h")]
+SOURCES = [os.path.join(PKG, "csrc", "fwi_engine.cu"), os.path.join(PKG, "csrc", "fwi_aux.cu")]
+DEPS = SOURCES + [os.path.join(PKG, "csrc", n) for n in ("fwi_kernels.cuh", "fwi_aux.cuh", "fwi_aux_kernels.cuh", "cpu_emu.h")] + \
+    [os.path.join(ROOT, "include", "fwi_gb300.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -42,14 +42,20 @@ struct dim3 {
     dim3(unsigned a = 1, unsigned b = 1, unsigned c = 1) : x(a), y(b), z(c) {}
 };
 struct int2 { int x, y; };
+struct alignas(8) float2 { float x, y; };
 struct alignas(16) float4 { float x, y, z, w; };
 inline int2 make_int2(int a, int b) { return int2{a, b}; }
+inline float2 make_float2(float a, float b) { return float2{a, b}; }
+inline float4 make_float4(float a, float b, float c, float d) { return float4{a, b, c, d}; }
 
 inline thread_local dim3 threadIdx, blockIdx, blockDim, gridDim;
 
 using std::max;
 using std::min;
 inline float __fmul_rn(float a, float b) { return a * b; }
+inline float __fadd_rn(float a, float b) { return a + b; }
+inline float __fsub_rn(float a, float b) { return a - b; }
+inline float __fdiv_rn(float a, float b) { return a / b; }
 template <class T> inline T __ldg(const T* p) { return *p; }
 template <class T> inline T __ldcg(const T* p) { return *p; }
 template <class T> inline void __stcg(T* p, T v) { *p = v; }
@@ -64,14 +70,14 @@ namespace fwi_emu {
 
 struct Pool {
     int nthreads = 0;
-    std::vector<std::thread> workers;
     std::barrier<>* bar = nullptr;                 // __syncthreads
     std::vector<std::barrier<>*> warp_bar;         // __shfl_*_sync
     std::vector<double> shfl;                      // one slot per thread
     std::function<void()> body;
     unsigned long long epoch = 0;
     int done = 0;
-    bool quit = false;
+    int gen = 0;                                   // workers of an older generation exit
+    int exiting = 0;                               // old workers that have not exited yet
     std::mutex m;
     std::condition_variable cv, cv_done;
     dim3 bdim, gdim, bidx;
@@ -79,7 +85,7 @@ struct Pool {
 
 inline Pool& pool()
 {
-    static Pool* p = new Pool;   // never destroyed: detached workers may still wait on it at exit
+    static Pool* p = new Pool;   // never destroyed: idle workers may still wait on it at exit
     return *p;
 }
 
@@ -91,16 +97,18 @@ inline std::vector<unsigned char>& dyn_buf()
 }
 inline unsigned char* dyn_smem() { return dyn_buf().data(); }
 
-inline void worker(int tid)
+inline void worker(int tid, int gen, unsigned long long seen)
 {
     Pool& P = pool();
-    unsigned long long seen = 0;
     for (;;) {
         std::function<void()> body;
         {
             std::unique_lock<std::mutex> lk(P.m);
-            P.cv.wait(lk, [&] { return P.quit || P.epoch != seen; });
-            if (P.quit) return;
+            P.cv.wait(lk, [&] { return P.gen != gen || P.epoch != seen; });
+            if (P.gen != gen) {
+                if (--P.exiting == 0) P.cv_done.notify_all();
+                return;
+            }
             seen = P.epoch;
             body = P.body;
             blockDim = P.bdim;
@@ -111,33 +119,32 @@ inline void worker(int tid)
         body();
         {
             std::lock_guard<std::mutex> lk(P.m);
-            if (++P.done == P.nthreads) P.cv_done.notify_one();
+            if (++P.done == P.nthreads) P.cv_done.notify_all();
         }
     }
 }
 
+// A pool of n workers; the workers of a pool of another size exit first.
 inline void ensure_pool(int n)
 {
     Pool& P = pool();
     if (P.nthreads == n) return;
     if (P.nthreads) {
-        {
-            std::lock_guard<std::mutex> lk(P.m);
-            P.quit = true;
-        }
+        std::unique_lock<std::mutex> lk(P.m);
+        P.exiting = P.nthreads;
+        ++P.gen;
         P.cv.notify_all();
-        std::this_thread::sleep_for(std::chrono::milliseconds(50));   // detached workers leave their wait
+        P.cv_done.wait(lk, [&] { return P.exiting == 0; });
         delete P.bar;
         for (auto* b : P.warp_bar) delete b;
         P.warp_bar.clear();
-        P.quit = false;
     }
     P.nthreads = n;
     P.bar = new std::barrier<>(n);
     for (int w = 0; w < (n + 31) / 32; ++w) P.warp_bar.push_back(new std::barrier<>(std::min(32, n - 32 * w)));
     P.shfl.assign(n, 0.0);
     for (int t = 0; t < n; ++t) {
-        std::thread th(worker, t);
+        std::thread th(worker, t, P.gen, P.epoch);
         th.detach();           // idle workers end with the process
     }
 }
@@ -175,7 +182,10 @@ inline int linear_tid() { return (int)(threadIdx.x + blockDim.x * (threadIdx.y +
 
 inline void __syncthreads() { fwi_emu::pool().bar->arrive_and_wait(); }
 
-inline double __shfl_xor_sync(unsigned, double v, int lane_mask)
+template <class T> inline T shfl_xor_emu(T v, int lane_mask);
+inline double __shfl_xor_sync(unsigned, double v, int lane_mask) { return shfl_xor_emu<double>(v, lane_mask); }
+inline float __shfl_xor_sync(unsigned, float v, int lane_mask) { return (float)shfl_xor_emu<double>(v, lane_mask); }
+template <class T> inline T shfl_xor_emu(T v, int lane_mask)
 {
     fwi_emu::Pool& P = fwi_emu::pool();
     const int t = fwi_emu::linear_tid(), w = t / 32;

@@ -7,6 +7,7 @@
 // every time step of every shot is one launch (grid.z = shot).
 #include "fwi_gb300.h"
 #include "fwi_kernels.cuh"
+#include "fwi_aux.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -122,6 +123,13 @@ struct fwi_ctx {
     std::vector<int> nt_slot;      // nt of each slot, descending
     long long nsamples = 0;
     int npartial = 0;
+    // misfit of fwi_gradient; XCORR works per shot on its traces
+    fwi_misfit msf{};
+    float4* geo_d = nullptr;       // per trace: source x, z, receiver x, z (metres)
+    float2* xpart_d = nullptr;     // per trace: XCORR misfit terms
+    std::vector<long long> shot_syn_off;          // per shot (input order): first sample of its traces
+    std::vector<int> shot_tr0, shot_nr, shot_nt0; // first trace, traces, samples per trace
+    int ntraces = 0;
     bool have_model = false, have_obs = false, have_fwd = false;
     size_t bytes_model = 0, bytes_shots = 0;
     std::string err;
@@ -175,11 +183,13 @@ void free_shots(fwi_ctx* x)
 {
     drop_graph(x);
     void* ps[] = {x->F, x->A, x->Gacc, x->psiF, x->psiA, x->ring, x->syn, x->res, x->obs, x->wav,
-                  x->shots_d, x->samp_d, x->recs_d, x->rtile_d, x->partial, x->mis};
+                  x->shots_d, x->samp_d, x->recs_d, x->rtile_d, x->partial, x->mis, x->geo_d, x->xpart_d};
     for (void* p : ps) if (p) cudaFree(p);
     x->F = x->A = x->Gacc = x->psiF = x->psiA = x->ring = x->syn = x->res = x->obs = x->wav = nullptr;
     x->shots_d = nullptr; x->samp_d = nullptr; x->recs_d = nullptr; x->rtile_d = nullptr;
-    x->partial = nullptr; x->mis = nullptr;
+    x->partial = nullptr; x->mis = nullptr; x->geo_d = nullptr; x->xpart_d = nullptr;
+    x->shot_syn_off.clear(); x->shot_tr0.clear(); x->shot_nr.clear(); x->shot_nt0.clear();
+    x->ntraces = 0;
     x->samp_off.clear();
     x->nshots = 0; x->nt_run = 0; x->nsamples = 0; x->bytes_shots = 0;
     x->nt_slot.clear();
@@ -385,6 +395,23 @@ int run_forward(fwi_ctx* x)
 
 int run_misfit(fwi_ctx* x)
 {
+    if (x->msf.kind == FWI_MISFIT_XCORR) {
+        // XCORR1D shot by shot (traces of one shot share their length), one sum over all traces
+        for (size_t s = 0; s < x->shot_nr.size(); ++s) {
+            if (!x->shot_nr[s]) continue;
+            const long long o = x->shot_syn_off[s];
+            launch_xcorr_traces(x->obs + o, x->syn + o, x->res + o, x->geo_d + x->shot_tr0[s],
+                                x->xpart_d + x->shot_tr0[s], x->shot_nr[s], x->shot_nt0[s], x->msf.offset_min,
+                                x->msf.offset_max, x->msf.slice, x->st);
+            DIAG_SYNC("k_xcorr");
+            ++x->stats.launches;
+        }
+        launch_xcorr_sum(x->xpart_d, x->ntraces, x->mis, x->st);
+        DIAG_SYNC("k_xcorr_sum");
+        CK(cudaGetLastError());
+        x->stats.launches += 1;
+        return FWI_OK;
+    }
     FWI_LAUNCH(k_misfit, x->npartial, 256, 0, x->st, x->syn, x->obs, x->res, x->nsamples, x->partial);
     DIAG_SYNC("k_misfit");
     FWI_LAUNCH(k_misfit_final, 1, 256, 0, x->st, x->partial, x->npartial, x->mis);
@@ -477,6 +504,14 @@ int run_phase(fwi_ctx* x, int ph, bool graph)
     }
     CK(cudaEventRecord(x->ev[evs[ph][1]], x->st));
     return FWI_OK;
+}
+
+// Traces longer than the XCORR kernel's shared memory holds?
+bool xcorr_too_long(const fwi_ctx* x)
+{
+    for (int nt0 : x->shot_nt0)
+        if (xcorr_smem_bytes(nt0) > XCORR_MAX_SMEM) return true;
+    return false;
 }
 
 }  // namespace
@@ -719,6 +754,9 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     std::vector<std::vector<Rec>> recs(nshots);
     long long syn_off = 0, wav_tot = 0;
     std::vector<long long> wav_off(nshots);
+    std::vector<long long> tr_syn_off(nshots);
+    std::vector<int> tr0(nshots), tr_nr(nshots), tr_nt0(nshots);
+    std::vector<float4> geo;                      // per trace, input order (XCORR offsets)
     for (int s = 0; s < nshots; ++s) {
         const fwi_shot& sh = shots[s];
         if (sh.nt < 1 || sh.nt > x->cfg.nt_max || (sh.nt - 1) % jump != 0)
@@ -746,6 +784,12 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
                 return fail(x, FWI_ERR_GEOMETRY, "shot " + std::to_string(s) + ": receiver " + std::to_string(r) + " outside the model");
             recs[s][r] = {(long long)(rz + g.z0p) * g.ld + rx + g.x0p, syn_off + (long long)r * d.nt0};
         }
+        tr_syn_off[s] = syn_off;
+        tr0[s] = (int)geo.size();
+        tr_nr[s] = sh.nr;
+        tr_nt0[s] = d.nt0;
+        for (int r = 0; r < sh.nr; ++r)
+            geo.push_back(make_float4(sh.src_x, sh.src_z, sh.rec_xz[2 * r], sh.rec_xz[2 * r + 1]));
         syn_off += (long long)sh.nr * d.nt0;
     }
     // slots: shots sorted by nt, longest first, so the active shots of a step form a prefix
@@ -819,6 +863,8 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     e = e ? e : dalloc(x, &x->rtile_d, rt_all.size(), &b);
     e = e ? e : dalloc(x, &x->partial, (size_t)x->npartial, &b);
     e = e ? e : dalloc(x, &x->mis, 2, &b);
+    e = e ? e : dalloc(x, &x->geo_d, geo.size(), &b);
+    e = e ? e : dalloc(x, &x->xpart_d, geo.size(), &b);
     if (e) { std::string m = x->err; free_shots(x); x->err = m; return e; }
     CK(cudaMemcpyAsync(x->shots_d, slot.data(), sizeof(ShotDev) * nshots, cudaMemcpyHostToDevice, x->st));
     if (!samp.empty()) {
@@ -827,6 +873,16 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     }
     CK(cudaMemcpyAsync(x->rtile_d, rt_all.data(), sizeof(int) * rt_all.size(), cudaMemcpyHostToDevice, x->st));
     CK(cudaMemcpyAsync(x->wav, wav_all.data(), sizeof(float) * wav_all.size(), cudaMemcpyHostToDevice, x->st));
+    if (!geo.empty()) CK(cudaMemcpyAsync(x->geo_d, geo.data(), sizeof(float4) * geo.size(), cudaMemcpyHostToDevice, x->st));
+    x->shot_syn_off = tr_syn_off;
+    x->shot_tr0 = tr0;
+    x->shot_nr = tr_nr;
+    x->shot_nt0 = tr_nt0;
+    x->ntraces = (int)geo.size();
+    if (x->msf.kind == FWI_MISFIT_XCORR && xcorr_too_long(x)) {
+        free_shots(x);
+        return fail(x, FWI_ERR_ARG, "traces too long for the XCORR kernel");
+    }
     CK(cudaMemsetAsync(x->syn, 0, sizeof(float) * std::max<long long>(1, syn_off), x->st));
 #ifdef FWI_SELF_CHECK
     {
@@ -997,6 +1053,26 @@ int fwi_l2_misfit_noalloc(const float* syn, const float* obs, float* residual, i
     FWI_LAUNCH(k_misfit_traces, ntraces, 256, 0, st, syn, obs, residual, nsamples, part);
     FWI_LAUNCH(k_misfit_final, 1, 256, 0, st, part, ntraces, misfit);
     if (cudaGetLastError() != cudaSuccess) return FWI_ERR_CUDA;
+    return FWI_OK;
+}
+
+int fwi_set_misfit(fwi_ctx* x, const fwi_misfit* m)
+{
+    if (!x || !m) return FWI_ERR_ARG;
+    if (m->kind != FWI_MISFIT_L2 && m->kind != FWI_MISFIT_XCORR)
+        return fail(x, FWI_ERR_ARG, "unknown misfit kind");
+    if (m->kind == FWI_MISFIT_XCORR && m->slice != FWI_XCORR_MIDDLE && m->slice != FWI_XCORR_LEADING)
+        return fail(x, FWI_ERR_ARG, "unknown XCORR slice");
+    CK(cudaSetDevice(x->cfg.device));
+    if (m->kind == FWI_MISFIT_XCORR) {
+        if (xcorr_too_long(x)) return fail(x, FWI_ERR_ARG, "traces too long for the XCORR kernel");
+        CK(xcorr_setup());
+    }
+    x->msf = *m;
+    // the captured misfit phase depends on the kind
+    if (x->gexec[1]) { cudaGraphExecDestroy(x->gexec[1]); x->gexec[1] = nullptr; }
+    if (x->graph[1]) { cudaGraphDestroy(x->graph[1]); x->graph[1] = nullptr; }
+    x->have_fwd = false;
     return FWI_OK;
 }
 

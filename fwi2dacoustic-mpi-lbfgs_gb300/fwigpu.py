@@ -88,8 +88,22 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.fwi_cpml_profile.argtypes = [I, F, F, F, F, F, C.POINTER(F), C.POINTER(F)]
     lib.fwi_fd_coefficients.argtypes = [F, F, C.POINTER(F)]
     lib.fwi_cell_of.argtypes = [F, F, F, F, C.POINTER(I), C.POINTER(I)]
+    lib.fwi_set_misfit.argtypes = [P, C.POINTER(FwiMisfit)]
+    lib.fwi_grad_precond.argtypes = [C.POINTER(F), I, I, F, I, I, I, I, F, C.POINTER(I)]
+    lib.fwi_bandpass.argtypes = [C.POINTER(F), I, I, F, I, I, I, F, F, C.POINTER(F)]
+    lib.fwi_xcorr1d.argtypes = [C.POINTER(F), C.POINTER(F), I, I, C.POINTER(F), F, F, I, C.POINTER(F), C.POINTER(F)]
     _LIB = lib
     return lib
+
+
+class FwiMisfit(C.Structure):
+    """fwi_misfit (include/fwi_gb300.h)."""
+    _fields_ = [("kind", C.c_int), ("slice", C.c_int), ("offset_min", C.c_float), ("offset_max", C.c_float),
+                ("reserved", C.c_int * 4)]
+
+
+MISFIT_L2, MISFIT_XCORR = 0, 1
+XCORR_MIDDLE, XCORR_LEADING = 0, 1
 
 
 def _fp(a):
@@ -219,6 +233,13 @@ class Engine:
         self._check(self.lib.fwi_gradient_f32(self.ctx, _dp(mis), _fp(grad)), "fwi_gradient_f32")
         return float(mis[1]), grad
 
+    def set_misfit(self, kind=MISFIT_L2, slice=XCORR_MIDDLE, offset_min=0.0, offset_max=1.0e30):
+        """Misfit of gradient(): MISFIT_L2 (default) or MISFIT_XCORR (XCORR1D,
+        slice XCORR_MIDDLE / XCORR_LEADING, traces outside [offset_min,
+        offset_max] metres skipped)."""
+        m = FwiMisfit(kind, slice, offset_min, offset_max)
+        self._check(self.lib.fwi_set_misfit(self.ctx, C.byref(m)), "fwi_set_misfit")
+
     def set_stream(self, stream_ptr):
         """Run on the caller's cudaStream_t (an int handle, e.g. torch's
         ``torch.cuda.current_stream().cuda_stream``); None restores the own stream."""
@@ -238,6 +259,52 @@ class Engine:
             out.append(np.asarray(flat[o:o + n]).reshape(s.nr, s.nt0(self.cfg.jump)))
             o += n
         return out
+
+
+# ---- routines around the gradient (standalone, on the current device) ---------
+
+def _check_status(st, what):
+    if st != FWI_OK:
+        raise FwiError(st, what)
+
+
+def grad_precond(body, perc, rectx1, repeat1, rectx2, repeat2, alpha_grad, bottom):
+    """grad_precond_new5 (grad_prec.c:5-52) of a float32 gradient [mnz][mnx];
+    returns a new array."""
+    lib = load_library()
+    out = np.ascontiguousarray(body, dtype=np.float32).copy()
+    mnz, mnx = out.shape
+    bot = np.ascontiguousarray(bottom, dtype=np.int32)
+    if bot.shape != (mnx,):
+        raise ValueError("bottom must have one entry per column")
+    _check_status(lib.fwi_grad_precond(_fp(out), mnx, mnz, perc, rectx1, repeat1, rectx2, repeat2, alpha_grad,
+                                       bot.ctypes.data_as(C.POINTER(C.c_int))), "fwi_grad_precond")
+    return out
+
+
+def bandpass(traces, dt, phase, nphi, nplo, fhi, flo):
+    """sfbandpass (butterworth_filter.c:127-200) of float32 traces [nr][nt]."""
+    lib = load_library()
+    x = np.ascontiguousarray(traces, dtype=np.float32)
+    nr, nt = x.shape
+    out = np.zeros_like(x)
+    _check_status(lib.fwi_bandpass(_fp(x), nt, nr, dt, int(phase), nphi, nplo, fhi, flo, _fp(out)), "fwi_bandpass")
+    return out
+
+
+def xcorr1d(obs, syn, sr_xyz, offset_min, offset_max, slice=XCORR_MIDDLE):
+    """XCORR1D (xcorr_msf.c:4-181) of float32 traces [nr][nt]; returns
+    (misfit[2], res[nr][nt])."""
+    lib = load_library()
+    o = np.ascontiguousarray(obs, dtype=np.float32)
+    sy = np.ascontiguousarray(syn, dtype=np.float32)
+    sr = np.ascontiguousarray(sr_xyz, dtype=np.float32)
+    nr, nt = o.shape
+    mis = np.zeros(2, np.float32)
+    res = np.zeros_like(o)
+    _check_status(lib.fwi_xcorr1d(_fp(o), _fp(sy), nr, nt, _fp(sr), offset_min, offset_max, slice, _fp(mis),
+                                  _fp(res)), "fwi_xcorr1d")
+    return mis, res
 
 
 # ---- host-only helpers (no device needed) ----------------------------------------

@@ -119,12 +119,31 @@ int fwi_forward(fwi_ctx *ctx, float *syn_out);
  * current model. */
 int fwi_backward(fwi_ctx *ctx, const float *residual, double *grad_out);
 
-/* Whole gradient on the device: forward, L2 misfit + residual (the missing
- * L2norm of msf_pool.h:1 / Mpar.h:68), backward, FP64 reduction.
- * misfit[0] = misfit[1] = 1/2 sum (syn - obs)^2 (msf->val[0..1],
- * MBotOpt.c:61,88).  grad_out [nz][nx] host, or NULL to keep it on the device
- * (fwi_grad_device). */
+/* Whole gradient on the device: forward, misfit + residual, backward, FP64
+ * reduction.  With the default L2 misfit (the missing L2norm of
+ * msf_pool.h:1 / Mpar.h:68) misfit[0] = misfit[1] = 1/2 sum (syn - obs)^2
+ * (msf->val[0..1], MBotOpt.c:61,88); with FWI_MISFIT_XCORR (fwi_set_misfit)
+ * they are XCORR1D's misfit[0..1] (xcorr_msf.c:56-131) and the residual is
+ * d misfit[1] / d syn.  grad_out [nz][nx] host, or NULL to keep it on the
+ * device (fwi_grad_device). */
 int fwi_gradient(fwi_ctx *ctx, double *misfit, double *grad_out);
+
+/* Misfit of fwi_gradient (the misfit pool of the reference's fwi_init,
+ * fwi_2d.c:194-213, par_xcorr1d header.h:309-315). */
+#define FWI_MISFIT_L2 0
+#define FWI_MISFIT_XCORR 1
+#define FWI_XCORR_MIDDLE 0     /* conv_how_to_slice "middle" */
+#define FWI_XCORR_LEADING 1    /* conv_how_to_slice "leading" */
+typedef struct {
+    int kind;                  /* FWI_MISFIT_L2 or FWI_MISFIT_XCORR */
+    int slice;                 /* XCORR: FWI_XCORR_MIDDLE or FWI_XCORR_LEADING */
+    float offset_min;          /* XCORR: traces whose source-receiver offset (metres, from */
+    float offset_max;          /* the shot geometry) lies outside [min, max] are skipped */
+    int reserved[4];           /* zero */
+} fwi_misfit;
+/* FWI_ERR_ARG for an unknown kind or slice, or XCORR traces longer than its
+ * shared-memory limit (about 11,000 samples). */
+int fwi_set_misfit(fwi_ctx *ctx, const fwi_misfit *misfit);
 
 /* Same as fwi_gradient, float gradient (plan->grad->body is float). */
 int fwi_gradient_f32(fwi_ctx *ctx, double *misfit, float *grad_out);
@@ -167,6 +186,35 @@ int fwi_version(void);
 #define FWI_NOALLOC_MAX_TRACES 65536
 int fwi_l2_misfit_noalloc(const float *syn, const float *obs, float *residual, int ntraces, int nsamples,
                           double *misfit, void *stream);
+
+/* ---- routines around the gradient (standalone, host buffers) ---------- */
+/* Each runs on the current device, allocates its device buffers for the call
+ * and returns when the result is back in host memory. */
+
+/* grad_precond_new5 (grad_prec.c:5-52) of body[mnz][mnx] in place: clip to
+ * perc * (min, max) unless perc == 0, triangle2(rectx1, rectx1, repeat1)
+ * (triangle_smooth.c:70-110), zero the cells above bottom[ix],
+ * triangle2(rectx2, rectx2, repeat2), scale by alpha_grad.  Bit-identical to
+ * the reference.  (fwi_grad's rectz1 / rectz2 are unused by the reference.) */
+int fwi_grad_precond(float *body, int mnx, int mnz, float perc, int rectx1, int repeat1, int rectx2, int repeat2,
+                     float alpha_grad, const int *bottom);
+
+/* sfbandpass (butterworth_filter.c:127-200): Butterworth low-cut at flo and
+ * high-cut at fhi (Hz) of nr traces of nt samples ([nr][nt]) with sample
+ * interval dt; phase != 0 filters once (minimum phase), phase == 0 forward
+ * and backward with half the orders (zero phase).  Bit-identical to the
+ * reference.  FWI_ERR_ARG for flo < 0 (where the reference exits) or orders
+ * above 32. */
+int fwi_bandpass(const float *indat, int nt, int nr, float dt, int phase, int nphi, int nplo, float fhi, float flo,
+                 float *outdat);
+
+/* XCORR1D (xcorr_msf.c:4-181) of nr traces of nt samples ([nr][nt]);
+ * sr_xyz = source x, z, then receiver x, z pairs (metres); slice
+ * FWI_XCORR_MIDDLE or FWI_XCORR_LEADING.  misfit[2] and res[nr][nt] as the
+ * reference; the correlations are exact sums (the reference's FFTs agree to
+ * their rounding). */
+int fwi_xcorr1d(const float *obs, const float *syn, int nr, int nt, const float *sr_xyz, float offset_min,
+                float offset_max, int slice, float *misfit, float *res);
 
 /* ---- host-only helpers (no device needed) ------------------------------ */
 /* Validates a configuration without touching a device. */

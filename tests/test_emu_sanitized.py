@@ -59,3 +59,17 @@ def test_emulated_gradient_is_memory_safe_and_matches_oracle(emu_lib, oracles, f
     assert out["syn_rel"] <= SYN_TOL, out
     assert abs(out["J"] - out["J64"]) <= 1e-5 * out["J64"], out
     assert out["grad_rel"] <= GRAD_TOL, out
+
+
+def test_emulated_aux_routines_are_memory_safe_and_match_oracle(emu_lib, oracles):
+    """fwi_grad_precond / fwi_bandpass bit-identical to the oracle, fwi_xcorr1d
+    and the XCORR gradient within tolerance (tests/aux_cases.py)."""
+    lib, libs = emu_lib
+    env = dict(os.environ, FWI_LIB=lib, LD_PRELOAD=" ".join(libs),
+               ASAN_OPTIONS="detect_leaks=0:abort_on_error=1", UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1")
+    r = subprocess.run([sys.executable, os.path.join(HERE, "emu_aux_case.py")], capture_output=True, text=True,
+                       env=env, timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-6000:]
+    assert "ERROR: AddressSanitizer" not in r.stderr and "runtime error" not in r.stderr, r.stderr[-6000:]
+    assert r.stdout.strip().splitlines()[-1] == "ok"
+

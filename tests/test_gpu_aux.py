@@ -1,0 +1,68 @@
+"""GPU parity of the routines around the gradient (tests/aux_cases.py):
+gradient preconditioning and Butterworth band-pass bit-identical to the
+oracle (and so to the reference), XCORR1D and the XCORR gradient within
+tolerance, at test sizes and at the C2 grid / trace sizes."""
+import numpy as np
+import pytest
+
+import aux_cases as A
+from conftest import ricker
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def aux(oracles, engine_lib):
+    return oracles[0].AuxOracle()
+
+
+def test_grad_precond_bit_exact(aux):
+    import fwigpu
+    A.check_precond(fwigpu, aux, big=True)
+
+
+def test_bandpass_bit_exact(aux):
+    import fwigpu
+    A.check_bandpass(fwigpu, aux, big=True)
+
+
+def test_xcorr1d(aux):
+    import fwigpu
+    A.check_xcorr(fwigpu, aux)
+
+
+def test_xcorr_long_traces(aux):
+    """C2-length traces (nt0 = 2001), both slices, against the oracle."""
+    import fwigpu
+    rng = np.random.default_rng(23)
+    nr, nt = 12, 2001
+    obs = rng.standard_normal((nr, nt)).astype(np.float32)
+    syn = (np.roll(obs, 5, axis=1) + 0.5 * rng.standard_normal((nr, nt))).astype(np.float32)
+    sr = np.concatenate([[0, 0], np.stack([np.arange(nr) * 50.0, np.full(nr, 2.0)], 1).ravel()]).astype(np.float32)
+    for mode in (0, 1):
+        m1, r1 = fwigpu.xcorr1d(obs, syn, sr, 0.0, 1e9, mode)
+        m2, r2 = aux.xcorr1d(obs, syn, sr, 0.0, 1e9, mode)
+        assert np.allclose(m1, m2, rtol=A.XCORR_MISFIT_RTOL, atol=0), (m1, m2)
+        assert A.rel(r1, r2) <= A.XCORR_RES_RTOL
+
+
+def test_engine_gradient_with_xcorr(oracles, aux):
+    import fwigpu
+    from test_gpu_parity import Case
+    O = oracles[0]
+    near = [(50, 1, np.arange(30, 72, 2), np.zeros(21, int), ricker(301, 0.001, 15.0)),
+            (100, 20, np.arange(80, 121, 4), np.full(11, 15), ricker(261, 0.001, 12.0))]
+    case = Case(O, 1, seed=41, nx=150, nz=90, shots=near)
+    A.check_engine_xcorr(fwigpu, aux, case)
+
+
+def test_misfit_argument_errors(engine_lib):
+    import fwigpu
+    cfg = fwigpu.make_config(40, 30, 10.0, 10.0, 0.001, 101, npml=8)
+    with fwigpu.Engine(cfg) as e:
+        with pytest.raises(fwigpu.FwiError):
+            e.set_misfit(7)
+        with pytest.raises(fwigpu.FwiError):
+            e.set_misfit(fwigpu.MISFIT_XCORR, 3)
+    assert fwigpu.STATUS[fwigpu.load_library().fwi_bandpass(None, 10, 1, 0.001, 0, 4, 4, 30.0, 3.0, None)] == \
+        "FWI_ERR_ARG"
