@@ -92,6 +92,13 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.fwi_grad_precond.argtypes = [C.POINTER(F), I, I, F, I, I, I, I, F, C.POINTER(I)]
     lib.fwi_bandpass.argtypes = [C.POINTER(F), I, I, F, I, I, I, F, F, C.POINTER(F)]
     lib.fwi_xcorr1d.argtypes = [C.POINTER(F), C.POINTER(F), I, I, C.POINTER(F), F, F, I, C.POINTER(F), C.POINTER(F)]
+    lib.fwi_lbfgs_create.argtypes = [C.c_longlong, C.POINTER(FwiLbfgsParam), C.POINTER(I)]
+    lib.fwi_lbfgs_create.restype = P
+    lib.fwi_lbfgs_destroy.argtypes = [P]
+    lib.fwi_lbfgs_destroy.restype = None
+    lib.fwi_lbfgs_begin.argtypes = [P, C.POINTER(D), D, P, I, C.POINTER(I)]
+    lib.fwi_lbfgs_next.argtypes = [P, C.POINTER(D), D, P, I, C.POINTER(I)]
+    lib.fwi_lbfgs_info.argtypes = [P, C.POINTER(I), C.POINTER(D), C.POINTER(I)]
     _LIB = lib
     return lib
 
@@ -102,6 +109,13 @@ class FwiMisfit(C.Structure):
                 ("reserved", C.c_int * 4)]
 
 
+class FwiLbfgsParam(C.Structure):
+    """fwi_lbfgs_param (include/fwi_gb300.h); defaults of lbfgs.h:77-79."""
+    _fields_ = [("m", C.c_int), ("epsilon", C.c_double), ("max_iterations", C.c_int), ("max_linesearch", C.c_int),
+                ("ftol", C.c_double), ("wolfe", C.c_double)]
+
+
+LBFGS_SUCCESS, LBFGS_MAXLINESEARCH, LBFGS_MAXITERATION, LBFGS_EVALUATE = 0, 1, 2, 3
 MISFIT_L2, MISFIT_XCORR = 0, 1
 XCORR_MIDDLE, XCORR_LEADING = 0, 1
 
@@ -305,6 +319,61 @@ def xcorr1d(obs, syn, sr_xyz, offset_min, offset_max, slice=XCORR_MIDDLE):
     _check_status(lib.fwi_xcorr1d(_fp(o), _fp(sy), nr, nt, _fp(sr), offset_min, offset_max, slice, _fp(mis),
                                   _fp(res)), "fwi_xcorr1d")
     return mis, res
+
+
+class Lbfgs:
+    """The device L-BFGS optimizer (MBotOpt.c:55-214, FP64) with reverse
+    communication::
+
+        opt = Lbfgs(n)
+        x = x0.copy(); f, g = evaluate(x)
+        state = opt.begin(x, f, g)            # x now holds the first trial point
+        while state == LBFGS_EVALUATE:
+            f, g = evaluate(x)
+            state = opt.next(x, f, g)         # next trial point, or the final point
+
+    g is a float64 host array, or an int device pointer (e.g.
+    Engine.grad_device_ptr()) of n float64 values."""
+
+    def __init__(self, n, m=12, epsilon=1e-9, max_iterations=8, max_linesearch=6, ftol=1e-7, wolfe=0.98):
+        self.lib = load_library()
+        self.n = int(n)
+        p = FwiLbfgsParam(m, epsilon, max_iterations, max_linesearch, ftol, wolfe)
+        st = C.c_int(0)
+        self.h = self.lib.fwi_lbfgs_create(self.n, C.byref(p), C.byref(st))
+        if not self.h:
+            raise FwiError(st.value, "fwi_lbfgs_create")
+
+    def close(self):
+        if self.h:
+            self.lib.fwi_lbfgs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _call(self, fn, x, f, g):
+        if x.dtype != np.float64 or not x.flags.c_contiguous or x.size != self.n:
+            raise ValueError("x must be a contiguous float64 array of n values")
+        if isinstance(g, int):
+            gp, dev = C.c_void_p(g), 1
+        else:
+            g = np.ascontiguousarray(g, dtype=np.float64)
+            gp, dev = C.c_void_p(g.ctypes.data), 0
+        state = C.c_int(-1)
+        _check_status(fn(self.h, _dp(x), float(f), gp, dev, C.byref(state)), fn.__name__)
+        return state.value
+
+    def begin(self, x, f, g):
+        return self._call(self.lib.fwi_lbfgs_begin, x, f, g)
+
+    def next(self, x, f, g):
+        return self._call(self.lib.fwi_lbfgs_next, x, f, g)
+
+    def info(self):
+        k, ne, step = C.c_int(), C.c_int(), C.c_double()
+        _check_status(self.lib.fwi_lbfgs_info(self.h, C.byref(k), C.byref(step), C.byref(ne)), "fwi_lbfgs_info")
+        return {"iteration": k.value, "step": step.value, "evaluations": ne.value}
 
 
 # ---- host-only helpers (no device needed) ----------------------------------------

@@ -216,6 +216,40 @@ int fwi_bandpass(const float *indat, int nt, int nr, float dt, int phase, int np
 int fwi_xcorr1d(const float *obs, const float *syn, int nr, int nt, const float *sr_xyz, float offset_min,
                 float offset_max, int slice, float *misfit, float *res);
 
+/* ---- L-BFGS optimizer (MBotOpt.c:55-214) on the device, FP64 ----------- */
+/* The reference's driver with reverse communication: the caller evaluates
+ * the objective f and gradient g at the point the optimizer returns in x,
+ * then passes them to fwi_lbfgs_next, which takes MBotOpt's line-search
+ * decision: Armijo (f > finit + step ftol dginit -> step *= 0.5), curvature
+ * (g.d < wolfe dginit -> step *= 2.1), strong curvature (g.d > -wolfe dginit
+ * -> step *= 0.5), at most max_linesearch trials; after an accepted step the
+ * test |g| / |x| <= epsilon, the iteration limit, the correction pair and
+ * the two-loop recursion over the last min(m, k) pairs; next first step 0.2
+ * for k < 4, else the mean of the last two accepted steps.  x and the state
+ * are FP64; g may be a device pointer (for example fwi_grad_device). */
+typedef struct {
+    int m;                     /* correction pairs kept (lbfgs.h:64) */
+    double epsilon;            /* |g| / |x| convergence threshold */
+    int max_iterations;        /* 0: no limit */
+    int max_linesearch;        /* trials per line search */
+    double ftol;               /* Armijo constant */
+    double wolfe;              /* curvature constant */
+} fwi_lbfgs_param;             /* NULL: the reference's defaults {12, 1e-9, 8, 6, 1e-7, 0.98} (lbfgs.h:77-79) */
+#define FWI_LBFGS_SUCCESS 0            /* LBFGS_SUCCESS: converged, x is the solution */
+#define FWI_LBFGS_MAXLINESEARCH 1      /* LBFGSERR_MAXIMUMLINESEARCH */
+#define FWI_LBFGS_MAXITERATION 2       /* LBFGSERR_MAXIMUMITERATION */
+#define FWI_LBFGS_EVALUATE 3           /* evaluate f and g at x, then call fwi_lbfgs_next */
+typedef struct fwi_lbfgs fwi_lbfgs;
+fwi_lbfgs *fwi_lbfgs_create(long long n, const fwi_lbfgs_param *param, int *status);
+void fwi_lbfgs_destroy(fwi_lbfgs *opt);
+/* x [n]: in, the start point (f, g evaluated there); out, the first trial point. */
+int fwi_lbfgs_begin(fwi_lbfgs *opt, double *x, double f, const double *g, int g_on_device, int *state);
+/* f, g at the last trial point; x out: the next trial point (state
+ * FWI_LBFGS_EVALUATE) or the final point (the other states). */
+int fwi_lbfgs_next(fwi_lbfgs *opt, double *x, double f, const double *g, int g_on_device, int *state);
+/* iteration k (MBotOpt's k), the current step, objective evaluations so far */
+int fwi_lbfgs_info(const fwi_lbfgs *opt, int *iteration, double *step, int *evaluations);
+
 /* ---- host-only helpers (no device needed) ------------------------------ */
 /* Validates a configuration without touching a device. */
 int fwi_check_config(const fwi_config *cfg);

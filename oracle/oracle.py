@@ -400,3 +400,59 @@ class RefAux(_AuxCalls):
         out = np.zeros_like(x)
         self.lib.sfbandpass(_ptr(x, C.c_float), nt, nr, dt, bool(phase), nphi, nplo, fhi, flo, _ptr(out, C.c_float))
         return out
+
+
+# ---------------------------------------------------------------------------
+# L-BFGS driver of MBotOpt.c (fwi_oracle_lbfgs.c) and the reference run
+# ---------------------------------------------------------------------------
+LBFGS_DEFAULTS = dict(m=12, epsilon=1e-9, max_iterations=8, max_linesearch=6, ftol=1e-7, wolfe=0.98)  # lbfgs.h:77-79
+MBOTOPT_N = 601 * 3921           # NZ * NX of the reference's Mpar.h, the size MBotOpt.c optimises
+
+
+class LbfgsOracle:
+    """orc_lbfgs_run: MBotOpt.c's L-BFGS on the objective of lbfgs_objective.h;
+    twin "f32" reproduces the reference's float arithmetic, "f64" is the FP64
+    oracle of the device optimizer."""
+
+    def __init__(self, twin="f64"):
+        self.twin = twin
+        self.lib = lib = C.CDLL(os.path.join(BUILD, f"libfwioracle_lbfgs_{twin}.so"))
+        lib.orc_lbfgs_run.argtypes = [C.c_long, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double,
+                                      C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int)]
+        lib.orc_lbfgs_run.restype = C.c_int
+        real = C.c_float if twin == "f32" else C.c_double
+        self._np = np.float32 if twin == "f32" else np.float64
+        lib.orc_lbfgs_objective.argtypes = [C.c_long, C.POINTER(real), C.POINTER(real)]
+        lib.orc_lbfgs_objective.restype = C.c_double
+        self._real = real
+        lib.orc_lbfgs_x0.argtypes = [C.c_long, C.POINTER(C.c_double)]
+
+    def run(self, n, max_evals=200, **param):
+        p = dict(LBFGS_DEFAULTS, **param)
+        ft = np.zeros(max_evals)
+        x = np.zeros(n)
+        ne = C.c_int()
+        ret = self.lib.orc_lbfgs_run(n, p["m"], p["epsilon"], p["max_iterations"], p["max_linesearch"], p["ftol"],
+                                     p["wolfe"], max_evals, _ptr(ft, C.c_double), _ptr(x, C.c_double), C.byref(ne))
+        return ret, ft[:min(ne.value, max_evals)], x
+
+    def objective(self, x):
+        x = np.ascontiguousarray(x, dtype=self._np)
+        g = np.zeros_like(x)
+        f = self.lib.orc_lbfgs_objective(len(x), _ptr(x, self._real), _ptr(g, self._real))
+        return f, g
+
+    def x0(self, n):
+        x = np.zeros(n)
+        self.lib.orc_lbfgs_x0(n, _ptr(x, C.c_double))
+        return x
+
+
+def run_reference_mbotopt(workdir):
+    """Runs the reference's own MBotOpt.c (oracle/_ref/mbotopt, single rank,
+    objective of lbfgs_objective.h) in workdir; returns (f trace, final x)."""
+    exe = os.path.join(REFDIR, "mbotopt")
+    trace = os.path.join(workdir, "trace.txt")
+    env = dict(os.environ, ORC_LBFGS_TRACE=trace)
+    subprocess.run([exe, "x"], cwd=workdir, env=env, check=True, stdout=subprocess.DEVNULL)
+    return np.loadtxt(trace, ndmin=1), np.fromfile(trace + ".x", np.float32)

@@ -97,3 +97,31 @@ def check_engine_xcorr(fwigpu, aux, case):
         assert abs(J2 - want) <= 1e-5 * want
     finally:
         e.close()
+
+
+LBFGS_RTOL = 1e-9    # FP64 both sides; only the order of the dot-product sums differs
+
+
+def check_lbfgs(fwigpu, O, n, **param):
+    """The device optimizer, fed by the FP64 oracle's objective, takes the
+    same trial points, objective values and termination as orc_lbfgs_run."""
+    o64 = O.LbfgsOracle("f64")
+    p = dict(O.LBFGS_DEFAULTS, **param)
+    ret, ftrace, x_want = o64.run(n, max_evals=5000, **param)
+    opt = fwigpu.Lbfgs(n, **p)
+    try:
+        x = o64.x0(n)
+        f, g = o64.objective(x)
+        got = [f]
+        state = opt.begin(x, f, g)
+        while state == fwigpu.LBFGS_EVALUATE and len(got) < 5000:
+            f, g = o64.objective(x)
+            got.append(f)
+            state = opt.next(x, f, g)
+        assert state == ret, (state, ret)
+        assert len(got) == len(ftrace), (len(got), len(ftrace))
+        assert np.allclose(got, ftrace, rtol=LBFGS_RTOL, atol=0)
+        assert rel(x, x_want) <= LBFGS_RTOL
+        assert opt.info()["evaluations"] == len(ftrace)
+    finally:
+        opt.close()

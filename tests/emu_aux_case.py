@@ -21,6 +21,7 @@ aux = O.AuxOracle()
 A.check_precond(fwigpu, aux)
 A.check_bandpass(fwigpu, aux)
 A.check_xcorr(fwigpu, aux)
+A.check_lbfgs(fwigpu, O, 3000)
 # a short record: receivers near the sources so that no trace is all zeros
 # (XCORR1D divides by the trace's correlation energy, as the reference does)
 from conftest import ricker  # noqa: E402

@@ -11,7 +11,8 @@ write_bdr / write_bdr_fs_no, and a full forward + boundary-strip rebuild
 (a_lap_opt_2d_pml + time_integral forward, read_bdr + a_lap_opt_2d +
 time_integral backward, chunked through a temporary file) on a small free-surface
 case, and ``tests/golden/ref_aux.npz``: outputs of grad_precond_new5,
-sfbandpass and XCORR1D (``--aux`` writes only this file).  The inputs are
+sfbandpass, XCORR1D and of MBotOpt.c's L-BFGS run on the objective of
+oracle/lbfgs_objective.h (``--aux`` writes only this file).  The inputs are
 regenerated from the seeds stored alongside.
 """
 from __future__ import annotations
@@ -65,6 +66,9 @@ BANDPASS_CASES = [(0.002, 0, 6, 6, 30.0, 3.0), (0.001, 1, 5, 3, 60.0, 5.0), (0.0
 XCORR_CASES = [(0, 50.0, 550.0, "pulse"), (1, 0.0, 1.0e9, "noise"), (0, 0.0, 1.0e9, "noise")]
 
 
+LBFGS_SAMPLE = 997               # the L-BFGS fixture keeps every 997th entry of the final model
+
+
 def aux_inputs():
     """Deterministic inputs of the preconditioning, band-pass and XCORR cases."""
     rng = np.random.default_rng(SEED + 7)
@@ -106,6 +110,13 @@ def main_aux() -> None:
     for k, (mode, omin, omax, kind) in enumerate(XCORR_CASES):
         o, sy, s_r = xcorr_traces(kind)
         out[f"xcorr_mis_{k}"], out[f"xcorr_res_{k}"] = ref.xcorr1d(o, sy, s_r, omin, omax, mode, npad=5)
+    # the reference's own MBotOpt.c on the objective of oracle/lbfgs_objective.h
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        ftrace, x = O.run_reference_mbotopt(td)
+    out["lbfgs_ftrace"] = ftrace.astype(np.float32)
+    out["lbfgs_x_sample"] = x[::LBFGS_SAMPLE]
+    out["lbfgs_x_sum"] = np.array([x.astype(np.float64).sum()])
     path = os.path.join(HERE, "ref_aux.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes")

@@ -66,3 +66,44 @@ def test_misfit_argument_errors(engine_lib):
             e.set_misfit(fwigpu.MISFIT_XCORR, 3)
     assert fwigpu.STATUS[fwigpu.load_library().fwi_bandpass(None, 10, 1, 0.001, 0, 4, 4, 30.0, 3.0, None)] == \
         "FWI_ERR_ARG"
+
+
+def test_lbfgs_matches_oracle(oracles):
+    """The reference's settings (8 iterations) and a run to convergence."""
+    import fwigpu
+    O = oracles[0]
+    A.check_lbfgs(fwigpu, O, 20000)
+    A.check_lbfgs(fwigpu, O, 5000, max_iterations=500)
+
+
+def test_lbfgs_on_the_fwi_gradient(oracles):
+    """Two L-BFGS iterations of FWI: the gradient stays on the device
+    (fwi_grad_device) and the objective decreases."""
+    import fwigpu
+    from test_gpu_parity import Case
+    O = oracles[0]
+    case = Case(O, 1, seed=51)
+    e = case.engine()
+    try:
+        e.set_model(case.vtrue)
+        obs = e.forward()
+        e.set_observed(obs)
+        x = case.vel.astype(np.float64).ravel().copy()
+        opt = fwigpu.Lbfgs(x.size, max_iterations=2)
+
+        def evaluate(xv):
+            e.set_model(xv.reshape(case.vel.shape).astype(np.float32))
+            J, _ = e.gradient(keep_on_device=True)
+            return J
+
+        J0 = evaluate(x)
+        state = opt.begin(x, J0, e.grad_device_ptr())
+        evals = [J0]
+        while state == fwigpu.LBFGS_EVALUATE and len(evals) < 40:
+            evals.append(evaluate(x))
+            state = opt.next(x, evals[-1], e.grad_device_ptr())
+        assert state in (fwigpu.LBFGS_MAXITERATION, fwigpu.LBFGS_SUCCESS), state
+        assert evals[-1] < evals[0]
+        opt.close()
+    finally:
+        e.close()
