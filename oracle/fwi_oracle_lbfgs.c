@@ -59,6 +59,11 @@ int orc_lbfgs_run(long n, int m, double epsilon, int max_iterations, int max_lin
     real *alpha = calloc(m, sizeof(real)), *ysv = calloc(m, sizeof(real));
     real *step_arr = calloc(max_iterations + 2, sizeof(real));
     int ret = -1, ne = 0, k = 1, end = 0;
+    if (!x || !xp || !g || !gp || !d || !S || !Y || !alpha || !ysv || !step_arr) {
+        free(x); free(xp); free(g); free(gp); free(d); free(S); free(Y); free(alpha); free(ysv); free(step_arr);
+        *nevals = 0;
+        return -3;
+    }
     real fx, step, width = 0, dg, finit, dginit, dgtest, ys, yy, xnorm, gnorm, beta;
     for (long i = 0; i < n; ++i) x[i] = (real)obj_x0(i);
     memset(S, 0, sizeof(real) * n * m);
