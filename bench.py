@@ -127,9 +127,17 @@ def traffic_per_cell_step(kernel):
     return None
 
 
-def workload(args):
+def workload(args, world=1, rank=0):
+    """The workload's shots; on world > 1 ranks, rank's cost-balanced share of
+    world x nshots shots (shots_parallel.partition_shots)."""
     import workloads
-    return workloads.build(args.workload, scale=args.scale, nshots=args.nshots, nt=args.nt)
+    per_rank = args.nshots or workloads.CONFIGS[args.workload]["nshots"]
+    cfgkw, vtrue, vstart, shots = workloads.build(args.workload, scale=args.scale, nshots=per_rank * world, nt=args.nt)
+    if world > 1:
+        import shots_parallel
+        mine = shots_parallel.partition_shots([s.nt for s in shots], world, rank)
+        shots = [shots[i] for i in mine]
+    return cfgkw, vtrue, vstart, shots
 
 
 def describe(args, cfgkw, shots):
@@ -227,7 +235,7 @@ def run_ours(args):
         dist.barrier()
     import fwigpu
 
-    cfgkw, vtrue, vstart, shots = workload(args)
+    cfgkw, vtrue, vstart, shots = workload(args, world, rank)
     nshots = len(shots)
     cfg = fwigpu.make_config(**cfgkw, device=local, use_graph=0 if args.no_graph else 1)
     eng = fwigpu.Engine(cfg)
@@ -246,19 +254,19 @@ def run_ours(args):
         if dist:
             dist.barrier()
 
-    grad_t = None
+    grad_t = mis_t = None
     if dist:
-        # the gradient lives in the engine; all ranks sum their shot partitions in FP64
-        class _View:
-            def __init__(self, ptr, n):
-                self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 2}
-        grad_t = torch.as_tensor(_View(eng.grad_device_ptr(), int(cells)), device=f"cuda:{local}")
+        # the gradient lives in the engine; the ranks sum their shot shares in FP64
+        import shots_parallel
+        grad_t = shots_parallel.device_tensor(eng.grad_device_ptr(), int(cells), f"cuda:{local}")
+        mis_t = torch.zeros(2, dtype=torch.float64, device=f"cuda:{local}")
 
     def step():
         J, _ = eng.gradient(keep_on_device=True)
         if dist:
             with torch.cuda.stream(stream):
-                dist.all_reduce(grad_t)
+                mis_t.fill_(J)
+                shots_parallel.allreduce_gradient(grad_t, mis_t)
         return J
 
     for _ in range(max(3, args.warmup)):
