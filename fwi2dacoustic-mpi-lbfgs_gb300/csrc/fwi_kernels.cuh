@@ -108,7 +108,6 @@ constexpr int UW = TX + 3;         // u positions x0-1 .. x0+TX+1
 constexpr int UWP = TX + 4;        // u row pitch
 constexpr int RXW = TX + 6;        // adjoint x-stage positions x0-3 .. x0+TX+2
 constexpr int RXP = TX + 8;
-constexpr int MX = 8;              // zero margin columns left of the grid in HBM arrays
 constexpr int MZ = 4;              // zero margin rows above the grid
 constexpr int NSTRIP = 3;          // 2*mm-1 saved rows/columns per side (fwi_sys.h:7, mm = 2)
 
@@ -119,6 +118,8 @@ struct Geo {
     int x0p, z0p;      // physical origin in padded coordinates
     int ld;            // row pitch of every field array (floats)
     int ntx, ntz;      // tiles per shot
+    int xoff;          // padded column of tile column 0 (<= 0): the tile grid starts where the
+                       // first interior tile can start, so general tiles hold few columns
     long long fstride; // floats between consecutive shots in a field array
 };
 
@@ -394,7 +395,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
     const float amp = *GP(P.wav + sd.wav_off + P.step) * cf.iarea;
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
-        if (GX && x0 + BX * h >= g.pnx) continue;                          // column half past the grid
+        if (GX && (x0 + BX * h >= g.pnx || x0 + BX * h + BX <= 0)) continue;   // column half outside the grid
         const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);        // this half needs the x-general formulas
         const int cl = tx + BX * h, c = x0 + cl;
         // every global operand of this column segment first: K, p^{it-1} and the psi entries
@@ -402,7 +403,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i;
-            const bool inside = (!GZ || row < g.pnz) && (!GX || c < g.pnx);
+            const bool inside = (!GZ || row < g.pnz) && (!GX || (c >= 0 && c < g.pnx));
             const long long o = (long long)row * g.ld + c;
             kq[i] = inside ? __ldg(GP(K + o)) : 0.f;
             po[i] = inside ? *GP(pold + o) : 0.f;
@@ -484,7 +485,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                 }
             }
             #undef UR
-            const bool inside = (!GZ || row < g.pnz) && (!GX || c < g.pnx);
+            const bool inside = (!GZ || row < g.pnz) && (!GX || (c >= 0 && c < g.pnx));
             if (gxc && inside) {
                 const PsiSite t = psi_ux(P, row, c);                      // fwi_2d.c:838-842
                 if (t.idx >= 0) {
@@ -528,10 +529,38 @@ __global__ void __launch_bounds__(NTH) k_fwd_gen(const StepParams P)
     if (P.step >= sd.nt) return;
     const Geo& g = P.g;
     const int2 t = *GP(P.gen_tiles + blockIdx.x);
-    const int x0 = t.x * TX, z0 = t.y * TZ;
+    const int x0 = g.xoff + t.x * TX, z0 = t.y * TZ;
     stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
     __syncthreads();
     fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su);
+}
+
+// Plain x stage of an interior tile: u = c0 (p[j] - p[j-1]) + c1 (p[j+1] - p[j-2])
+// (ADJ false) or its transpose ubar = c0 (q[j-1] - q[j]) + c1 (q[j-2] - q[j+1])
+// (ADJ true) at the UW u positions j = x0 - 1 + jj of the TZ rows, from the
+// staged tile st into su.  Each warp computes the first 2 BX positions of its
+// rows with all lanes busy; the UW - 2 BX halo positions of all rows follow
+// in one pass spread over the block.
+template <bool ADJ>
+__device__ __forceinline__ void x_stage_plain(const float* st, float* su, const Coef& cf)
+{
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    [[maybe_unused]] constexpr int NS = SPH * SPW, NU = TZ * UWP;
+    constexpr int XH = UW - 2 * BX;
+    auto one = [&](int rl, int jj) {
+        const int q = (rl + HZ) * SPW + HX - 1 + jj;                      // st index of column j
+        float v;
+        if (!ADJ) v = cf.c0x * (st[SIDX(q, NS)] - st[SIDX(q - 1, NS)]) + cf.c1x * (st[SIDX(q + 1, NS)] - st[SIDX(q - 2, NS)]);
+        else      v = cf.c0x * (st[SIDX(q - 1, NS)] - st[SIDX(q, NS)]) + cf.c1x * (st[SIDX(q - 2, NS)] - st[SIDX(q + 1, NS)]);
+        su[SIDX(rl * UWP + jj, NU)] = v;
+    };
+    #pragma unroll
+    for (int k = 0; k < R; ++k) {
+        #pragma unroll
+        for (int h = 0; h < 2; ++h) one(ty + BY * k, tx + BX * h);
+    }
+    const int t = ty * BX + tx;
+    if (t < XH * TZ) one(t / XH, 2 * BX + t % XH);
 }
 
 // Forward step, interior tiles: no edge, CPML or strip cells, so every cell
@@ -546,7 +575,7 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_fast(const StepParams P)
     if (P.step >= nt) return;
     const Geo& g = P.g;
     const Coef& cf = P.c;
-    const int x0 = (P.fast_tx0 + blockIdx.x) * TX, z0 = (P.fast_tz0 + blockIdx.y) * TZ;
+    const int x0 = g.xoff + (P.fast_tx0 + blockIdx.x) * TX, z0 = (P.fast_tz0 + blockIdx.y) * TZ;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const long long so = (long long)s * g.fstride;
     float* __restrict__ pold = P.pold + so;
@@ -562,18 +591,7 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_fast(const StepParams P)
         }
     stage_tile(P.pcur + so, g, x0, z0, sp);
     __syncthreads();
-    #pragma unroll
-    for (int k = 0; k < R; ++k) {
-        const int rl = ty + BY * k;
-        #pragma unroll
-        for (int h = 0; h < 3; ++h) {
-            const int jj = tx + BX * h;
-            if (jj >= UW) break;
-            const int q = (rl + HZ) * SPW + HX - 1 + jj;                  // sp index of column j = x0 - 1 + jj
-            su[SIDX(rl * UWP + jj, TZ * UWP)] = cf.c0x * (sp[SIDX(q, SPH * SPW)] - sp[SIDX(q - 1, SPH * SPW)]) +
-                                                cf.c1x * (sp[SIDX(q + 1, SPH * SPW)] - sp[SIDX(q - 2, SPH * SPW)]);
-        }
-    }
+    x_stage_plain<false>(sp, su, cf);
     __syncthreads();
     const ShotDev sd = *GP(P.shots + s);
     const float amp = *GP(P.wav + sd.wav_off + P.step) * cf.iarea;
@@ -737,7 +755,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     float* __restrict__ bold = P.bold + so;
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
-        if (GX && x0 + BX * h >= pnx) continue;
+        if (GX && (x0 + BX * h >= pnx || x0 + BX * h + BX <= 0)) continue;   // column half outside the grid
         const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);        // this half needs the x-general formulas
         const int cl = tx + BX * h, c = x0 + cl;
         // every global operand of this column segment first: K, b^{m+2} and the psi entries
@@ -745,7 +763,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i;
-            const bool inside = (!GZ || row < pnz) && (!GX || c < pnx);
+            const bool inside = (!GZ || row < pnz) && (!GX || (c >= 0 && c < pnx));
             const long long o = (long long)row * g.ld + c;
             kq[i] = inside ? __ldg(GP(K + o)) : 0.f;
             bo[i] = inside ? *GP(bold + o) : 0.f;
@@ -856,7 +874,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             float pbar = px + pz;
             if (do_res) pbar += sm.racc[SIDX((r0l + i) * TX + cl, TZ * TX)];
             float b = 0.f;
-            if ((!GZ || row < pnz) && (!GX || c < pnx)) {
+            if ((!GZ || row < pnz) && (!GX || (c >= 0 && c < pnx))) {
                 const long long o = (long long)row * g.ld + c;
                 b = fmaf(kq[i], pbar, fmaf(2.f, qc[i + 3], -bo[i]));
                 *GP(bold + o) = b;
@@ -875,7 +893,7 @@ __global__ void __launch_bounds__(NTH, 3) k_bwd_edge(const StepParams P)
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
     const Geo& g = P.g;
     const int2 t = *GP(P.gen_tiles + blockIdx.x);
-    const int x0 = t.x * TX, z0 = t.y * TZ;
+    const int x0 = g.xoff + t.x * TX, z0 = t.y * TZ;
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
     const int m = P.step;
@@ -1018,7 +1036,7 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
     const int m = P.step;
     if (m > sd.nt) return;
     const int txi = P.fast_tx0 + blockIdx.x, tzi = P.fast_tz0 + blockIdx.y;
-    const int x0 = txi * TX, z0 = tzi * TZ;
+    const int x0 = g.xoff + txi * TX, z0 = tzi * TZ;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
     const long long so = (long long)s * g.fstride;
     float* __restrict__ bold = P.bold + so;
@@ -1055,18 +1073,7 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
     __syncthreads();
 
     // adjoint, x: ubar[j] = c0 (q[j-1] - q[j]) + c1 (q[j-2] - q[j+1]) at u positions j in [x0-1, x0+TX+1]
-    #pragma unroll
-    for (int k = 0; k < R; ++k) {
-        const int rl = ty + BY * k;
-        #pragma unroll
-        for (int h = 0; h < 3; ++h) {
-            const int jj = tx + BX * h;
-            if (jj >= UW) break;
-            const int q0 = (rl + HZ) * SPW + HX - 1 + jj;         // sq index of column j = x0 - 1 + jj
-            sm.su[SIDX(rl * UWP + jj, NU)] = cf.c0x * (sm.sq[SIDX(q0 - 1, NS)] - sm.sq[SIDX(q0, NS)]) +
-                                             cf.c1x * (sm.sq[SIDX(q0 - 2, NS)] - sm.sq[SIDX(q0 + 1, NS)]);
-        }
-    }
+    x_stage_plain<true>(sm.sq, sm.su, cf);
     __syncthreads();
 
     // adjoint, z chain in registers, and b^m = 2 b^{m+1} - b^{m+2} + K (L^T b^{m+1} + r^m)
@@ -1105,18 +1112,7 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
             ga[h * R + i] = __ldcg(GP(gacc + o));
         }
     __syncthreads();
-    #pragma unroll
-    for (int k = 0; k < R; ++k) {
-        const int rl = ty + BY * k;
-        #pragma unroll
-        for (int h = 0; h < 3; ++h) {
-            const int jj = tx + BX * h;
-            if (jj >= UW) break;
-            const int p0 = (rl + HZ) * SPW + HX - 1 + jj;             // sp index of column j = x0 - 1 + jj
-            sm.su[SIDX(rl * UWP + jj, NU)] = cf.c0x * (sm.sp[SIDX(p0, NS)] - sm.sp[SIDX(p0 - 1, NS)]) +
-                                             cf.c1x * (sm.sp[SIDX(p0 + 1, NS)] - sm.sp[SIDX(p0 - 2, NS)]);
-        }
-    }
+    x_stage_plain<false>(sm.sp, sm.su, cf);
     __syncthreads();
 
     // rebuild p^{m-2} = 2 p^{m-1} - p^m + K (L p^{m-1} + s^{m-1}) and imaging g += b^m (L p^{m-1} + f^{m-1})
