@@ -578,16 +578,18 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_fast(const StepParams P)
     const int x0 = g.xoff + (P.fast_tx0 + blockIdx.x) * TX, z0 = (P.fast_tz0 + blockIdx.y) * TZ;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const long long so = (long long)s * g.fstride;
-    float* __restrict__ pold = P.pold + so;
     const int r0l = R * ty, r0 = z0 + r0l;
+    // this thread's cells: rows r0 + i, columns x0 + tx + BX h, at 32-bit offsets i ld + BX h
+    const long long o0 = (long long)r0 * g.ld + x0 + tx;
+    float* __restrict__ prow = P.pold + so + o0;
+    const float* __restrict__ krow = P.K + o0;
     float po[CX * R], kk[CX * R];
     #pragma unroll
     for (int h = 0; h < CX; ++h)
         #pragma unroll
         for (int i = 0; i < R; ++i) {
-            const long long o = (long long)(r0 + i) * g.ld + x0 + tx + BX * h;
-            po[h * R + i] = __ldcg(GP(pold + o));
-            kk[h * R + i] = __ldg(GP(P.K + o));
+            po[h * R + i] = __ldcg(GP(prow + i * g.ld + BX * h));
+            kk[h * R + i] = __ldg(GP(krow + i * g.ld + BX * h));
         }
     stage_tile(P.pcur + so, g, x0, z0, sp);
     __syncthreads();
@@ -595,6 +597,7 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_fast(const StepParams P)
     __syncthreads();
     const ShotDev sd = *GP(P.shots + s);
     const float amp = *GP(P.wav + sd.wav_off + P.step) * cf.iarea;
+    const bool src_tile = sd.src_r >= z0 && sd.src_r < z0 + TZ && sd.src_c >= x0 && sd.src_c < x0 + TX;   // uniform
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
         const int cl = tx + BX * h, c = x0 + cl;
@@ -613,8 +616,8 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_fast(const StepParams P)
                              cf.c1x * (su[SIDX(u0 + 2, TZ * UWP)] - su[SIDX(u0 - 1, TZ * UWP)]);
             const float k1 = kk[h * R + i];
             float pn = fmaf(k1, ux + vz, fmaf(2.f, pc[i + 3], -po[h * R + i]));
-            if (row == sd.src_r && c == sd.src_c) pn += amp * k1;
-            __stcg(GP(pold + (long long)row * g.ld + c), pn);
+            if (src_tile && row == sd.src_r && c == sd.src_c) pn += amp * k1;
+            __stcg(GP(prow + i * g.ld + BX * h), pn);
         }
     }
 }
@@ -1117,6 +1120,7 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
 
     // rebuild p^{m-2} = 2 p^{m-1} - p^m + K (L p^{m-1} + s^{m-1}) and imaging g += b^m (L p^{m-1} + f^{m-1})
     const float f = *GP(P.wav + sd.wav_off + m - 1) * cf.iarea;
+    const bool src_tile = sd.src_r >= z0 && sd.src_r < z0 + TZ && sd.src_c >= x0 && sd.src_c < x0 + TX;   // uniform
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
         const int cl = tx + BX * h, c = x0 + cl;
@@ -1136,7 +1140,7 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
                              cf.c1x * (sm.su[SIDX(u0 + 2, NU)] - sm.su[SIDX(u0 - 1, NU)]);
             float lp = ux + vz;
             float pn = fmaf(kk[q], lp, fmaf(2.f, pc[i + 3], -pm[q]));
-            if (row == sd.src_r && c == sd.src_c) { pn += f * kk[q]; lp += f; }
+            if (src_tile && row == sd.src_r && c == sd.src_c) { pn += f * kk[q]; lp += f; }
             __stcg(GP(pold + o), pn);
             __stcg(GP(gacc + o), fmaf(bm[q], lp, ga[q]));
         }
