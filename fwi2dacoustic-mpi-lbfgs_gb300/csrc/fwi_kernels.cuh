@@ -520,7 +520,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
 // Forward step, tiles of the general path (edges, CPML, strips) of one
 // class (GX, GZ), from the list P.gen_tiles.
 template <bool GX, bool GZ>
-__global__ void __launch_bounds__(NTH) k_fwd_gen(const StepParams P)
+__global__ void __launch_bounds__(NTH, 4) k_fwd_gen(const StepParams P)
 {
     __shared__ __align__(16) float sp[SPH * SPW];
     __shared__ __align__(16) float su[TZ * UWP];
@@ -566,7 +566,7 @@ __device__ __forceinline__ void x_stage_plain(const float* st, float* su, const 
 // Forward step, interior tiles: no edge, CPML or strip cells, so every cell
 // takes the same branch-free stencil.  The per-cell loads of p^{it-1} and K
 // are issued before the tile copy so that their latencies overlap.
-__global__ void __launch_bounds__(NTH, 4) k_fwd_fast(const StepParams P)
+__global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
 {
     __shared__ __align__(16) float sp[SPH * SPW];
     __shared__ __align__(16) float su[TZ * UWP];
@@ -890,7 +890,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
 // Backward step, tiles of the general path (edges, CPML, strips) of one
 // class (GX, GZ), from the list P.gen_tiles.
 template <bool GX, bool GZ>
-__global__ void __launch_bounds__(NTH, 3) k_bwd_edge(const StepParams P)
+__global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
 {
     FWI_DYN_SMEM(smraw);
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
