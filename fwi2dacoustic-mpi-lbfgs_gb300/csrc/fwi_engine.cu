@@ -611,19 +611,27 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     g.pnx = cfg->nx + 2 * cfg->npml;                         // fwi_2d.c:155
     g.pnz = cfg->nz + (g.fs ? 1 : 2) * cfg->npml;            // fwi_2d.c:155,162
     g.x0p = cfg->npml; g.z0p = g.fs ? 0 : cfg->npml;
-    g.ntx = (g.pnx + TX - 1) / TX;
+    // Tile grid in x: the first interior tile starts at the first column x0i
+    // (a multiple of 4, for 16-byte staging) whose stencils reach no edge,
+    // CPML or strip cell; tile column 0 starts xoff <= 0 columns earlier.
+    // The left zero margin mx covers the halo of that first tile, and makes
+    // every tile's staged rows start on a 128-byte boundary.
+    const int x0i = (int)round_up(std::max(8, g.npml + 5), 4);
+    g.xoff = x0i - TX * ((x0i + TX - 1) / TX);
+    const int mx = HX - g.xoff;                              // (mx + xoff - HX) == 0: aligned rows
+    g.ntx = (g.pnx - g.xoff + TX - 1) / TX;
     g.ntz = (g.pnz + TZ - 1) / TZ;
-    g.ld = (int)round_up(MX + (long long)g.ntx * TX + HX, 32);
+    g.ld = (int)round_up(mx + g.xoff + (long long)g.ntx * TX + HX, 32);
     x->rows_alloc = MZ + g.ntz * TZ + MZ;
     g.fstride = (long long)x->rows_alloc * g.ld;
-    x->origin = (long long)MZ * g.ld + MX;
+    x->origin = (long long)MZ * g.ld + mx;
 
     // interior tile rectangle and the list of general-path tiles
     {
         std::vector<int2> gen;
         int tx0 = -1, tx1 = -1, tz0 = -1, tz1 = -1;
         for (int t = 0; t < g.ntx; ++t)
-            if (!tile_x_general(g, t * TX)) { if (tx0 < 0) tx0 = t; tx1 = t + 1; }
+            if (!tile_x_general(g, g.xoff + t * TX)) { if (tx0 < 0) tx0 = t; tx1 = t + 1; }
         for (int t = 0; t < g.ntz; ++t)
             if (!tile_z_general(g, t * TZ)) { if (tz0 < 0) tz0 = t; tz1 = t + 1; }
         if (tx0 < 0 || tz0 < 0) tx0 = tx1 = tz0 = tz1 = 0;
@@ -633,7 +641,7 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
             for (int tz = 0; tz < g.ntz; ++tz)
                 for (int tx = 0; tx < g.ntx; ++tx) {
                     if (tx >= tx0 && tx < tx1 && tz >= tz0 && tz < tz1) continue;
-                    const bool gx = tile_x_general(g, tx * TX), gz = tile_z_general(g, tz * TZ);
+                    const bool gx = tile_x_general(g, g.xoff + tx * TX), gz = tile_z_general(g, tz * TZ);
                     if (!gx && !gz) return bail(FWI_ERR_ARG);     // cannot happen: such tiles form the rectangle
                     if ((gx && !gz && cls == 0) || (!gx && gz && cls == 1) || (gx && gz && cls == 2))
                         gen.push_back(make_int2(tx, tz));
@@ -820,10 +828,11 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
             const long long foff = recs[s][r].foff;
             samp.push_back(RecSample{k, 0, foff, recs[s][r].syn_base, 0});
             const int row = (int)(foff / g.ld), col = (int)(foff % g.ld);
+            const int cx = col - g.xoff;                     // column relative to tile column 0 (>= 0)
             RecDev rd{};
-            rd.cell = (row % TZ) * TX + (col % TX);
+            rd.cell = (row % TZ) * TX + (cx % TX);
             rd.syn_base = recs[s][r].syn_base;
-            tmp.push_back({(row / TZ) * g.ntx + col / TX, rd});
+            tmp.push_back({(row / TZ) * g.ntx + cx / TX, rd});
         }
         std::stable_sort(tmp.begin(), tmp.end(), [](const auto& a, const auto& b2) { return a.first < b2.first; });
         d.rtile_off = (int)rt_all.size();
