@@ -620,11 +620,18 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     g.xoff = x0i - TX * ((x0i + TX - 1) / TX);
     const int mx = HX - g.xoff;                              // (mx + xoff - HX) == 0: aligned rows
     g.ntx = (g.pnx - g.xoff + TX - 1) / TX;
-    g.ntz = (g.pnz + TZ - 1) / TZ;
+    // The same in z: the first interior tile starts at row z0i (a multiple
+    // of R, so the warp holding row 0 starts there, as the top formulas
+    // assume) and tile row 0 starts zoff <= 0 rows earlier, above a margin
+    // of MZ zero rows.
+    const int z0i = g.fs ? 8 : (int)round_up(std::max(8, g.npml + 5), R);
+    g.zoff = z0i - TZ * ((z0i + TZ - 1) / TZ);
+    const int mz = MZ - g.zoff;
+    g.ntz = (g.pnz - g.zoff + TZ - 1) / TZ;
     g.ld = (int)round_up(mx + g.xoff + (long long)g.ntx * TX + HX, 32);
-    x->rows_alloc = MZ + g.ntz * TZ + MZ;
+    x->rows_alloc = mz + g.zoff + g.ntz * TZ + MZ;
     g.fstride = (long long)x->rows_alloc * g.ld;
-    x->origin = (long long)MZ * g.ld + mx;
+    x->origin = (long long)mz * g.ld + mx;
 
     // interior tile rectangle and the list of general-path tiles
     {
@@ -633,7 +640,7 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
         for (int t = 0; t < g.ntx; ++t)
             if (!tile_x_general(g, g.xoff + t * TX)) { if (tx0 < 0) tx0 = t; tx1 = t + 1; }
         for (int t = 0; t < g.ntz; ++t)
-            if (!tile_z_general(g, t * TZ)) { if (tz0 < 0) tz0 = t; tz1 = t + 1; }
+            if (!tile_z_general(g, g.zoff + t * TZ)) { if (tz0 < 0) tz0 = t; tz1 = t + 1; }
         if (tx0 < 0 || tz0 < 0) tx0 = tx1 = tz0 = tz1 = 0;
         // general tiles grouped by class: 0 = x-general only, 1 = z-general only, 2 = both
         for (int cls = 0; cls < 3; ++cls) {
@@ -641,7 +648,7 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
             for (int tz = 0; tz < g.ntz; ++tz)
                 for (int tx = 0; tx < g.ntx; ++tx) {
                     if (tx >= tx0 && tx < tx1 && tz >= tz0 && tz < tz1) continue;
-                    const bool gx = tile_x_general(g, g.xoff + tx * TX), gz = tile_z_general(g, tz * TZ);
+                    const bool gx = tile_x_general(g, g.xoff + tx * TX), gz = tile_z_general(g, g.zoff + tz * TZ);
                     if (!gx && !gz) return bail(FWI_ERR_ARG);     // cannot happen: such tiles form the rectangle
                     if ((gx && !gz && cls == 0) || (!gx && gz && cls == 1) || (gx && gz && cls == 2))
                         gen.push_back(make_int2(tx, tz));
@@ -828,11 +835,11 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
             const long long foff = recs[s][r].foff;
             samp.push_back(RecSample{k, 0, foff, recs[s][r].syn_base, 0});
             const int row = (int)(foff / g.ld), col = (int)(foff % g.ld);
-            const int cx = col - g.xoff;                     // column relative to tile column 0 (>= 0)
+            const int cx = col - g.xoff, rz = row - g.zoff;  // relative to the tile grid's origin (>= 0)
             RecDev rd{};
-            rd.cell = (row % TZ) * TX + (cx % TX);
+            rd.cell = (rz % TZ) * TX + (cx % TX);
             rd.syn_base = recs[s][r].syn_base;
-            tmp.push_back({(row / TZ) * g.ntx + cx / TX, rd});
+            tmp.push_back({(rz / TZ) * g.ntx + cx / TX, rd});
         }
         std::stable_sort(tmp.begin(), tmp.end(), [](const auto& a, const auto& b2) { return a.first < b2.first; });
         d.rtile_off = (int)rt_all.size();

@@ -108,7 +108,7 @@ constexpr int UW = TX + 3;         // u positions x0-1 .. x0+TX+1
 constexpr int UWP = TX + 4;        // u row pitch
 constexpr int RXW = TX + 6;        // adjoint x-stage positions x0-3 .. x0+TX+2
 constexpr int RXP = TX + 8;
-constexpr int MZ = 4;              // zero margin rows above the grid
+constexpr int MZ = 4;              // zero margin rows above the first tile's halo and below the last tile
 constexpr int NSTRIP = 3;          // 2*mm-1 saved rows/columns per side (fwi_sys.h:7, mm = 2)
 
 struct Geo {
@@ -120,6 +120,7 @@ struct Geo {
     int ntx, ntz;      // tiles per shot
     int xoff;          // padded column of tile column 0 (<= 0): the tile grid starts where the
                        // first interior tile can start, so general tiles hold few columns
+    int zoff;          // padded row of tile row 0 (<= 0, a multiple of R), the same for rows
     long long fstride; // floats between consecutive shots in a field array
 };
 
@@ -157,7 +158,7 @@ struct alignas(16) RecSample {
 
 // One receiver for the backward injection, grouped by tile.
 struct alignas(16) RecDev {
-    int cell;                // (row % TZ) * TX + (col % TX) inside its tile
+    int cell;                // (row - z0) * TX + (col - x0) inside its tile at (z0, x0)
     int pad;
     long long syn_base;      // syn_off + r * nt0
 };
@@ -351,7 +352,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             #pragma unroll
             for (int h = 0; h < 3; ++h) {
                 const int jj = tx + BX * h;
-                const bool gen = jj < UW && !(GZ && row >= g.pnz) && x_window_general(g, x0 - 1 + BX * h, BX);
+                const bool gen = jj < UW && !(GZ && (row < 0 || row >= g.pnz)) && x_window_general(g, x0 - 1 + BX * h, BX);
                 pu[k][h] = gen ? psi_load(psr, psi_u(P, row, x0 - 1 + jj)) : 0.f;
             }
         }
@@ -359,7 +360,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
     #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int rl = ty + BY * k, row = z0 + rl;
-        if (GZ && row >= g.pnz) continue;                                   // rows past the grid
+        if (GZ && (row < 0 || row >= g.pnz)) continue;                      // rows outside the grid
         const int pbase = (rl + HZ) * SPW + HX - x0;                       // + global column = sp index
         #pragma unroll
         for (int h = 0; h < 3; ++h) {
@@ -388,7 +389,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
     __syncthreads();
 
     const int r0l = R * ty, r0 = z0 + r0l;
-    if (GZ && r0 >= g.pnz) return;                                         // the last phase: no barrier follows
+    if (GZ && (r0 < 0 || r0 >= g.pnz)) return;                             // the last phase: no barrier follows
     const bool gzw = GZ && z_window_general(g, r0, R);                     // this warp's rows need the z-general formulas
     const float* __restrict__ K = P.K;
     float* __restrict__ pold = P.pold + so;
@@ -529,7 +530,7 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_gen(const StepParams P)
     if (P.step >= sd.nt) return;
     const Geo& g = P.g;
     const int2 t = *GP(P.gen_tiles + blockIdx.x);
-    const int x0 = g.xoff + t.x * TX, z0 = t.y * TZ;
+    const int x0 = g.xoff + t.x * TX, z0 = g.zoff + t.y * TZ;
     stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
     __syncthreads();
     fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su);
@@ -575,7 +576,7 @@ __global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
     if (P.step >= nt) return;
     const Geo& g = P.g;
     const Coef& cf = P.c;
-    const int x0 = g.xoff + (P.fast_tx0 + blockIdx.x) * TX, z0 = (P.fast_tz0 + blockIdx.y) * TZ;
+    const int x0 = g.xoff + (P.fast_tx0 + blockIdx.x) * TX, z0 = g.zoff + (P.fast_tz0 + blockIdx.y) * TZ;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const long long so = (long long)s * g.fstride;
     const int r0l = R * ty, r0 = z0 + r0l;
@@ -677,7 +678,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         #pragma unroll
         for (int k = 0; k < R; ++k) {
             const int row = z0 + ty + BY * k;
-            const bool live = !(GZ && row >= pnz);
+            const bool live = !(GZ && (row < 0 || row >= pnz));
             #pragma unroll
             for (int h = 0; h < 3; ++h) {
                 const int ii = tx + BX * h, jj = ii;
@@ -693,7 +694,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         #pragma unroll
         for (int k = 0; k < R; ++k) {
             const int rl = ty + BY * k, row = z0 + rl;
-            if (GZ && row >= pnz) continue;
+            if (GZ && (row < 0 || row >= pnz)) continue;
             const int qrow = (rl + HZ) * SPW + HX - 3;        // sq index of column x0 - 3
             #pragma unroll
             for (int h = 0; h < 3; ++h) {
@@ -717,7 +718,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int rl = ty + BY * k, row = z0 + rl;
-        if (GZ && row >= pnz) continue;
+        if (GZ && (row < 0 || row >= pnz)) continue;
         #pragma unroll
         for (int h = 0; h < 3; ++h) {
             const int jj = tx + BX * h;
@@ -752,7 +753,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     __syncthreads();
 
     const int r0l = R * ty, r0 = z0 + r0l;
-    if (GZ && r0 >= pnz) return;                 // no rows of this thread exist; the caller skips them too
+    if (GZ && (r0 < 0 || r0 >= pnz)) return;     // no rows of this thread exist; the caller skips them too
     const bool gzw = GZ && z_window_general(g, r0, R);                     // this warp's rows need the z-general formulas
     const float* __restrict__ K = P.K;
     float* __restrict__ bold = P.bold + so;
@@ -812,8 +813,8 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 if (g.fs) {
                     if (kv >= 0 && kv <= 4) {
                         // vz[0] = (-22 v0 + 17 v1 + 9 v2 - 5 v3 + v4) iz24 (fwi_2d.c:848), transposed;
-                        // kv <= 4 only happens in the top tile (z0 == 0), where row 0 is sq row HZ
-                        const float r00 = sm.sq[SIDX(HZ * SPW + HX + cl, NS)];   // rbar[0] = q[0] (no top CPML)
+                        // kv <= 4 only happens in the top tile (z0 <= 0), where row 0 is sq row HZ - z0
+                        const float r00 = sm.sq[SIDX((HZ - z0) * SPW + HX + cl, NS)];   // rbar[0] = q[0] (no top CPML)
                         const float hcoef = (kv == 0) ? -22.f : (kv == 1) ? 17.f : (kv == 2) ? 9.f : (kv == 3) ? -5.f : 1.f;
                         v += hcoef * r00 * cf.iz24;
                     }
@@ -896,7 +897,7 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
     const Geo& g = P.g;
     const int2 t = *GP(P.gen_tiles + blockIdx.x);
-    const int x0 = g.xoff + t.x * TX, z0 = t.y * TZ;
+    const int x0 = g.xoff + t.x * TX, z0 = g.zoff + t.y * TZ;
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
     const int m = P.step;
@@ -937,7 +938,7 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
     #pragma unroll
     for (int k = 0; k < R; ++k) {
         const int rl = ty + BY * k;
-        if (GZ && z0 + rl >= zp1) continue;
+        if (GZ && (z0 + rl < zp0 || z0 + rl >= zp1)) continue;
         #pragma unroll
         for (int h = 0; h < 3; ++h) {
             const int jj = tx + BX * h;
@@ -1039,7 +1040,7 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
     const int m = P.step;
     if (m > sd.nt) return;
     const int txi = P.fast_tx0 + blockIdx.x, tzi = P.fast_tz0 + blockIdx.y;
-    const int x0 = g.xoff + txi * TX, z0 = tzi * TZ;
+    const int x0 = g.xoff + txi * TX, z0 = g.zoff + tzi * TZ;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
     const long long so = (long long)s * g.fstride;
     float* __restrict__ bold = P.bold + so;
