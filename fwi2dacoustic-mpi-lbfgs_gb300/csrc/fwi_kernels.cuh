@@ -222,7 +222,39 @@ __host__ __device__ inline bool z_window_general(const Geo& g, int z0, int h)
     return z0 < 8 || z0 + h + 8 > g.pnz || z0 + h + 4 >= g.pnz - np || (!g.fs && z0 - 4 <= np);
 }
 __host__ __device__ inline bool tile_x_general(const Geo& g, int x0) { return x_window_general(g, x0, TX); }
+// The w positions from j0 all lie outside [lo, hi]: in the x stages of the
+// tiles at the grid's ends, such windows have no psi site and a zero result.
+__device__ __forceinline__ bool x_window_outside(int j0, int w, int lo, int hi) { return j0 + w <= lo || j0 > hi; }
 __host__ __device__ inline bool tile_z_general(const Geo& g, int z0) { return z_window_general(g, z0, TZ); }
+
+// A z-general unit of R rows from r0 needs the grid-edge formulas (free
+// surface, one-sided differences at rows 0, 1, pnz-2, pnz-1, values outside
+// the grid) only near the top or bottom of the grid; elsewhere (a CPML band)
+// it takes the plain differences and the psi recursions.  The margins are the
+// reach of the adjoint's one-sided terms (rows r0-3 .. r0+R+2 against rows 1
+// and pnz-2, and the free-surface terms of rows up to 4), which is the wider.
+__device__ __forceinline__ bool z_unit_edge(const Geo& g, int r0) { return r0 < 8 || r0 + R + 4 > g.pnz; }
+
+// Work units of the z phases of a general tile: a row group of R rows and a
+// column half.  A tile with L row groups inside the padded grid has L * CX
+// units, and warp ty takes units ty and ty + BY (q = 0, 1).  In a full tile
+// (L == BY) that is the warp's own R rows in both halves; in a tile with few
+// live groups (the free-surface band above the interior has two) the units
+// spread over more warps, so the block holds its slot for a shorter time.
+struct ZUnit {
+    int r0l, h;        // first local row, column half
+    bool live;
+};
+template <bool GZ>
+__device__ __forceinline__ ZUnit z_unit(const Geo& g, int z0, int q)
+{
+    if (!GZ) return {R * (int)threadIdx.y, q, true};                       // tiles inside the grid in z
+    const int lo = max(z0, 0), hi = min(z0 + TZ, g.pnz);                   // z0 and 0 are multiples of R
+    const int gl0 = (lo - z0) / R, L = (hi - z0 + R - 1) / R - gl0;
+    const int u = threadIdx.y + BY * q;
+    if (u >= L * CX) return {0, 0, false};
+    return {R * (gl0 + u % L), u / L, true};
+}
 
 // CPML psi sites.  Each returns the offset of the psi entry within one shot's
 // psi block (or -1 where the position has none) and the profile node and
@@ -352,7 +384,8 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             #pragma unroll
             for (int h = 0; h < 3; ++h) {
                 const int jj = tx + BX * h;
-                const bool gen = jj < UW && !(GZ && (row < 0 || row >= g.pnz)) && x_window_general(g, x0 - 1 + BX * h, BX);
+                const bool gen = jj < UW && !(GZ && (row < 0 || row >= g.pnz)) && x_window_general(g, x0 - 1 + BX * h, BX) &&
+                                 !x_window_outside(x0 - 1 + BX * h, BX, 0, g.pnx);
                 pu[k][h] = gen ? psi_load(psr, psi_u(P, row, x0 - 1 + jj)) : 0.f;
             }
         }
@@ -372,6 +405,8 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                 const int q = pbase + j;
                 u = cf.c0x * (sp[SIDX(q, SPH * SPW)] - sp[SIDX(q - 1, SPH * SPW)]) +
                     cf.c1x * (sp[SIDX(q + 1, SPH * SPW)] - sp[SIDX(q - 2, SPH * SPW)]);
+            } else if (x_window_outside(x0 - 1 + BX * h, BX, 0, g.pnx)) {  // u positions are 0 .. pnx
+                u = 0.f;
             } else {
                 u = u_edge(sp, pbase, j, g.pnx, cf);
                 const PsiSite t = psi_u(P, row, j);                        // fwi_2d.c:790-794
@@ -388,14 +423,16 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
     }
     __syncthreads();
 
-    const int r0l = R * ty, r0 = z0 + r0l;
-    if (GZ && (r0 < 0 || r0 >= g.pnz)) return;                             // the last phase: no barrier follows
-    const bool gzw = GZ && z_window_general(g, r0, R);                     // this warp's rows need the z-general formulas
     const float* __restrict__ K = P.K;
     float* __restrict__ pold = P.pold + so;
     const float amp = *GP(P.wav + sd.wav_off + P.step) * cf.iarea;
     #pragma unroll
-    for (int h = 0; h < CX; ++h) {
+    for (int q = 0; q < CX; ++q) {
+        const ZUnit zu = z_unit<GZ>(g, z0, q);
+        if (!zu.live) continue;                                            // the last phase: no barrier follows
+        const int r0l = zu.r0l, r0 = z0 + r0l, h = zu.h;
+        const bool gzw = GZ && z_window_general(g, r0, R);                 // this unit's rows need the z-general formulas
+        const bool gze = gzw && z_unit_edge(g, r0);                        // ... and the grid-edge ones among them
         if (GX && (x0 + BX * h >= g.pnx || x0 + BX * h + BX <= 0)) continue;   // column half outside the grid
         const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);        // this half needs the x-general formulas
         const int cl = tx + BX * h, c = x0 + cl;
@@ -425,7 +462,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             if (!gzw) {
                 v = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
             } else {
-                if (kv >= 2 && kv <= g.pnz - 2) {
+                if (!gze || (kv >= 2 && kv <= g.pnz - 2)) {
                     v = cf.c0z * (pc[k + 2] - pc[k + 1]) + cf.c1z * (pc[k + 3] - pc[k]);
                 } else if (kv == 0) {                                     // fwi_2d.c:805 (here r0 == 0)
                     v = g.fs ? (3675.f * pc[3] - 1225.f * pc[4] + 441.f * pc[5] - 75.f * pc[6]) * cf.iz840 : 0.f;
@@ -457,7 +494,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             if (!gzw) {
                 vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
             } else {
-                if (row >= 1 && row <= g.pnz - 2) {
+                if (!gze || (row >= 1 && row <= g.pnz - 2)) {
                     vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
                 } else if (row == 0) {                                    // fwi_2d.c:848 (i == 0 here)
                     if (i == 0) {
@@ -682,8 +719,10 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             #pragma unroll
             for (int h = 0; h < 3; ++h) {
                 const int ii = tx + BX * h, jj = ii;
-                pux[k][h] = (live && ii < RXW) ? psi_load(psr, psi_ux(P, row, x0 - 3 + ii)) : 0.f;
-                const bool gen = live && jj < UW && x_window_general(g, x0 - 1 + BX * h, BX);
+                pux[k][h] = (live && ii < RXW && !x_window_outside(x0 - 3 + BX * h, BX, 0, pnx - 1))
+                                ? psi_load(psr, psi_ux(P, row, x0 - 3 + ii)) : 0.f;
+                const bool gen = live && jj < UW && x_window_general(g, x0 - 1 + BX * h, BX) &&
+                                 !x_window_outside(x0 - 1 + BX * h, BX, 0, pnx);
                 pu[k][h] = gen ? psi_load(psr, psi_u(P, row, x0 - 1 + jj)) : 0.f;
             }
         }
@@ -700,6 +739,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             for (int h = 0; h < 3; ++h) {
                 const int ii = tx + BX * h;
                 if (ii >= RXW) break;
+                if (x_window_outside(x0 - 3 + BX * h, BX, 0, pnx - 1)) continue;   // stage 2 reads cells 0 .. pnx-1
                 float r = sm.sq[SIDX(qrow + ii, NS)];
                 const PsiSite t = psi_ux(P, row, x0 - 3 + ii);
                 if (t.idx >= 0) {
@@ -729,6 +769,8 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 const int q0 = (rl + HZ) * SPW + HX - 1 + jj;     // sq index of column j
                 ub = cf.c0x * (sm.sq[SIDX(q0 - 1, NS)] - sm.sq[SIDX(q0, NS)]) +
                      cf.c1x * (sm.sq[SIDX(q0 - 2, NS)] - sm.sq[SIDX(q0 + 1, NS)]);
+            } else if (x_window_outside(x0 - 1 + BX * h, BX, 0, pnx)) {    // ubar positions are 0 .. pnx
+                ub = 0.f;
             } else {
                 const int rbase = rl * RXP + 3 - x0;             // + global column = srx index
                 #define RM(i) (((i) >= 1 && (i) <= pnx - 2) ? sm.srx[SIDX(rbase + (i), NR)] : 0.f)
@@ -752,13 +794,15 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     }
     __syncthreads();
 
-    const int r0l = R * ty, r0 = z0 + r0l;
-    if (GZ && (r0 < 0 || r0 >= pnz)) return;     // no rows of this thread exist; the caller skips them too
-    const bool gzw = GZ && z_window_general(g, r0, R);                     // this warp's rows need the z-general formulas
     const float* __restrict__ K = P.K;
     float* __restrict__ bold = P.bold + so;
     #pragma unroll
-    for (int h = 0; h < CX; ++h) {
+    for (int q = 0; q < CX; ++q) {
+        const ZUnit zu = z_unit<GZ>(g, z0, q);                              // the rebuild takes the same units
+        if (!zu.live) continue;
+        const int r0l = zu.r0l, r0 = z0 + r0l, h = zu.h;
+        const bool gzw = GZ && z_window_general(g, r0, R);                 // this unit's rows need the z-general formulas
+        const bool gze = gzw && z_unit_edge(g, r0);                        // ... and the grid-edge ones among them
         if (GX && (x0 + BX * h >= pnx || x0 + BX * h + BX <= 0)) continue;   // column half outside the grid
         const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);        // this half needs the x-general formulas
         const int cl = tx + BX * h, c = x0 + cl;
@@ -801,7 +845,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         for (int k = 0; k < R + 3; ++k) {
             const int kv = r0 - 1 + k;
             float v;
-            if (!gzw) {
+            if (!gze) {
                 v = cf.c0z * (rz[k + 1] - rz[k + 2]) + cf.c1z * (rz[k] - rz[k + 3]);
             } else {
                 // rz index of row q is q - (r0 - 3); row kv-1 -> k+1 etc.
@@ -824,6 +868,8 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 }
                 if (kv == pnz) v += cf.iz * rz[k + 1];
                 if (kv == pnz - 1) v -= cf.iz * rz[k + 2];
+            }
+            if (gzw) {
                 const PsiSite t = psi_v(P, kv, c);
                 if (t.idx >= 0) {
                     const float* ca = t.side ? a1z : a0z;
@@ -841,7 +887,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             const int ubase = (r0l + i) * UWP + 1 - x0;                   // + u position = su index
             #define UB(j) sm.su[SIDX(ubase + (j), NU)]
             float pz, px;
-            if (!gzw) {
+            if (!gze) {
                 pz = cf.c0z * (vb[i + 1] - vb[i + 2]) + cf.c1z * (vb[i] - vb[i + 3]);
             } else {
                 // vbar index of row q is q - (r0 - 1)
@@ -883,7 +929,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 b = fmaf(kq[i], pbar, fmaf(2.f, qc[i + 3], -bo[i]));
                 *GP(bold + o) = b;
             }
-            bm[h * R + i] = b;
+            bm[q * R + i] = b;
         }
     }
 }
@@ -949,15 +995,16 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
         }
     }
     __syncthreads();
-    const int r0l = R * ty, r0 = z0 + r0l;
-    if (GZ && (r0 >= zp1 || r0 + R <= zp0)) return;   // no physical row of this thread; no barrier follows
-    const bool gzw = GZ && z_window_general(g, r0, R);  // rows that may be outside the region or strips
     const float* __restrict__ K = P.K;
     float* __restrict__ pold = P.pold + so;
     float* __restrict__ gacc = P.gacc + so;
     const float f = *GP(P.wav + sd.wav_off + m - 1) * cf.iarea;
     #pragma unroll
-    for (int h = 0; h < CX; ++h) {
+    for (int q = 0; q < CX; ++q) {
+        const ZUnit zu = z_unit<GZ>(g, z0, q);               // adj_tile's units: bm[q] belongs to this one
+        const int r0l = zu.r0l, r0 = z0 + r0l, h = zu.h;
+        if (!zu.live || (GZ && (r0 >= zp1 || r0 + R <= zp0))) continue;   // no physical row; no barrier follows
+        const bool gzw = GZ && z_window_general(g, r0, R);  // rows that may be outside the region or strips
         if (GX && (x0 + BX * h >= xp1 || x0 + BX * h + BX <= xp0)) continue;   // no physical column in this half
         const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);
         const int cl = tx + BX * h, c = x0 + cl;
@@ -1006,7 +1053,7 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
                 lp = ((pm - 2.f * p1) + pn) / kk;
             }
             *GP(pold + o) = pn;
-            *GP(gacc + o) = fmaf(bm[h * R + i], lp, gq[i]);
+            *GP(gacc + o) = fmaf(bm[q * R + i], lp, gq[i]);
         }
     }
 }
