@@ -312,8 +312,29 @@ __device__ __forceinline__ float u_edge(const float* sp, int base, int j, int pn
     return 0.f;   // u[0], u[pnx] are never assigned by the reference
 }
 
-// Stages the (TZ+2HZ) x (TX+2HX) tile of field f whose interior starts at
-// (z0, x0) into shared memory with 16-byte loads.
+// 16-byte global -> shared copy that bypasses the registers (cp.async), so a
+// thread's copies of a tile are all in flight at once.  cp_async_wait()
+// completes the calling thread's copies; the barrier after it publishes the
+// tile to the block.  The CPU emulation copies at once.
+__device__ __forceinline__ void cp_async16(float* dst, const float4* src)
+{
+#ifdef FWI_CPU_EMU
+    *reinterpret_cast<float4*>(dst) = *src;
+#else
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src) : "memory");
+#endif
+}
+__device__ __forceinline__ void cp_async_wait()
+{
+#ifndef FWI_CPU_EMU
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+#endif
+}
+
+// Starts copying the (TZ+2HZ) x (TX+2HX) tile of field f whose interior
+// starts at (z0, x0) into shared memory in 16-byte pieces; cp_async_wait()
+// and a barrier must follow before the tile is read.
 __device__ __forceinline__ void stage_tile(const float* __restrict__ f, const Geo& g, int x0, int z0, float* sp)
 {
     const int tid = threadIdx.y * BX + threadIdx.x;
@@ -321,7 +342,7 @@ __device__ __forceinline__ void stage_tile(const float* __restrict__ f, const Ge
     for (int i = tid; i < SPH * Q; i += NTH) {
         const int r = i / Q, q = i - r * Q;
         const float4* src = reinterpret_cast<const float4*>(f + (long long)(z0 - HZ + r) * g.ld + (x0 - HX) + 4 * q);
-        *reinterpret_cast<float4*>(sp + SIDX(r * SPW + 4 * q, SPH * SPW)) = __ldg(GP(src));
+        cp_async16(sp + SIDX(r * SPW + 4 * q, SPH * SPW), GP(src));
     }
 }
 
@@ -569,6 +590,7 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_gen(const StepParams P)
     const int2 t = *GP(P.gen_tiles + blockIdx.x);
     const int x0 = g.xoff + t.x * TX, z0 = g.zoff + t.y * TZ;
     stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
+    cp_async_wait();
     __syncthreads();
     fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su);
 }
@@ -630,6 +652,7 @@ __global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
             kk[h * R + i] = __ldg(GP(krow + i * g.ld + BX * h));
         }
     stage_tile(P.pcur + so, g, x0, z0, sp);
+    cp_async_wait();
     __syncthreads();
     x_stage_plain<false>(sp, su, cf);
     __syncthreads();
@@ -973,6 +996,7 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
             atomicAdd(&sm.racc[SIDX(rd.cell, TZ * TX)], *GP(P.res + rd.syn_base + k));
         }
     }
+    cp_async_wait();
     __syncthreads();
 
     float bm[CX * R];
@@ -1121,6 +1145,7 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
             atomicAdd(&sm.racc[SIDX(rd.cell, TZ * TX)], *GP(P.res + rd.syn_base + k));
         }
     }
+    cp_async_wait();
     __syncthreads();
 
     // adjoint, x: ubar[j] = c0 (q[j-1] - q[j]) + c1 (q[j-2] - q[j+1]) at u positions j in [x0-1, x0+TX+1]
