@@ -119,6 +119,7 @@ struct fwi_ctx {
     int ngen = 0;
     int gen_off[4] = {};           // class c occupies gen_d[gen_off[c], gen_off[c + 1])
     int ftx0 = 0, ftx1 = 0, ftz0 = 0, ftz1 = 0;   // interior tile rectangle
+    int gen_arith = 0;             // gen_d agrees with gen_tile_at
     std::vector<int> samp_off;                    // per-slot ranges (nshots + 1)
     std::vector<int> nt_slot;      // nt of each slot, descending
     long long nsamples = 0;
@@ -208,6 +209,9 @@ StepParams base_params(const fwi_ctx* x)
     P.gen_tiles = x->gen_d;
     P.fast_tx0 = x->ftx0;
     P.fast_tz0 = x->ftz0;
+    P.fast_tx1 = x->ftx1;
+    P.fast_tz1 = x->ftz1;
+    P.gen_arith = x->gen_arith;
     P.recs = x->recs_d;
     P.rtile = x->rtile_d;
     P.wav = x->wav;
@@ -655,6 +659,12 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
                 }
         }
         x->gen_off[3] = (int)gen.size();
+        x->gen_arith = 1;                                   // the kernels may compute the tiles instead
+        for (int cls = 0; cls < 3; ++cls)
+            for (int i = x->gen_off[cls]; i < x->gen_off[cls + 1]; ++i) {
+                const int2 a = gen_tile_at(g, tx0, tx1, tz0, tz1, cls != 1, cls != 0, i - x->gen_off[cls]);
+                if (a.x != gen[i].x || a.y != gen[i].y) x->gen_arith = 0;
+            }
         x->ftx0 = tx0; x->ftx1 = tx1; x->ftz0 = tz0; x->ftz1 = tz1;
         x->ngen = (int)gen.size();
         if (dalloc(x, &x->gen_d, gen.size(), &x->bytes_model)) return bail(FWI_ERR_NOMEM);

@@ -188,7 +188,9 @@ struct StepParams {
     PsiLayout pl;
     const ShotDev* shots;
     const int2* gen_tiles;   // tiles of the general path (x tile, z tile)
-    int fast_tx0, fast_tz0;  // first interior tile of the branch-free path
+    int fast_tx0, fast_tz0;  // interior tile rectangle [fast_tx0, fast_tx1) x [fast_tz0, fast_tz1)
+    int fast_tx1, fast_tz1;
+    int gen_arith;           // general tiles follow from the rectangle (gen_tile_at), no list read
     const RecDev* recs;      // backward: receivers grouped by tile
     const int* rtile;        // backward: per-tile CSR of recs
     const float* wav;
@@ -234,6 +236,21 @@ __host__ __device__ inline bool tile_z_general(const Geo& g, int z0) { return z_
 // reach of the adjoint's one-sided terms (rows r0-3 .. r0+R+2 against rows 1
 // and pnz-2, and the free-surface terms of rows up to 4), which is the wider.
 __device__ __forceinline__ bool z_unit_edge(const Geo& g, int r0) { return r0 < 8 || r0 + R + 4 > g.pnz; }
+
+// Tile i of a general class, from the interior tile rectangle [tx0, tx1) x
+// [tz0, tz1): the x-general class is the general columns (left, then right)
+// of the interior rows, the z-general class the interior columns of the
+// general rows (top, then bottom), the corners the general columns of the
+// general rows, each row by row.  The engine checks this against its tile
+// lists; it spares every general block a dependent load before its copies.
+__host__ __device__ inline int2 gen_tile_at(const Geo& g, int tx0, int tx1, int tz0, int tz1, bool gx, bool gz, int i)
+{
+    const int ncol = gx ? g.ntx - (tx1 - tx0) : tx1 - tx0;
+    const int cx = i % ncol, cz = i / ncol;
+    const int tx = gx ? (cx < tx0 ? cx : cx - tx0 + tx1) : tx0 + cx;
+    const int tz = gz ? (cz < tz0 ? cz : cz - tz0 + tz1) : tz0 + cz;
+    return make_int2(tx, tz);
+}
 
 // Work units of the z phases of a general tile: a row group of R rows and a
 // column half.  A tile with L row groups inside the padded grid has L * CX
@@ -585,11 +602,13 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_gen(const StepParams P)
     __shared__ __align__(16) float su[TZ * UWP];
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
-    if (P.step >= sd.nt) return;
     const Geo& g = P.g;
-    const int2 t = *GP(P.gen_tiles + blockIdx.x);
+    const int2 t = P.gen_arith ? gen_tile_at(g, P.fast_tx0, P.fast_tx1, P.fast_tz0, P.fast_tz1, GX, GZ, blockIdx.x)
+                               : *GP(P.gen_tiles + blockIdx.x);
     const int x0 = g.xoff + t.x * TX, z0 = g.zoff + t.y * TZ;
     stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
+    // only active shots are launched; the test waits for nothing the copies need
+    if (P.step >= sd.nt) { cp_async_wait(); return; }
     cp_async_wait();
     __syncthreads();
     fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su);
@@ -631,8 +650,7 @@ __global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
     __shared__ __align__(16) float sp[SPH * SPW];
     __shared__ __align__(16) float su[TZ * UWP];
     const int s = blockIdx.z + P.shot_base;
-    const int nt = GP(P.shots + s)->nt;
-    if (P.step >= nt) return;
+    const ShotDev sd = *GP(P.shots + s);
     const Geo& g = P.g;
     const Coef& cf = P.c;
     const int x0 = g.xoff + (P.fast_tx0 + blockIdx.x) * TX, z0 = g.zoff + (P.fast_tz0 + blockIdx.y) * TZ;
@@ -652,11 +670,12 @@ __global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
             kk[h * R + i] = __ldg(GP(krow + i * g.ld + BX * h));
         }
     stage_tile(P.pcur + so, g, x0, z0, sp);
+    // only active shots are launched; the test comes after the loads are issued
+    if (P.step >= sd.nt) { cp_async_wait(); return; }
     cp_async_wait();
     __syncthreads();
     x_stage_plain<false>(sp, su, cf);
     __syncthreads();
-    const ShotDev sd = *GP(P.shots + s);
     const float amp = *GP(P.wav + sd.wav_off + P.step) * cf.iarea;
     const bool src_tile = sd.src_r >= z0 && sd.src_r < z0 + TZ && sd.src_c >= x0 && sd.src_c < x0 + TX;   // uniform
     #pragma unroll
@@ -965,12 +984,12 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
     FWI_DYN_SMEM(smraw);
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
     const Geo& g = P.g;
-    const int2 t = *GP(P.gen_tiles + blockIdx.x);
+    const int2 t = P.gen_arith ? gen_tile_at(g, P.fast_tx0, P.fast_tx1, P.fast_tz0, P.fast_tz1, GX, GZ, blockIdx.x)
+                               : *GP(P.gen_tiles + blockIdx.x);
     const int x0 = g.xoff + t.x * TX, z0 = g.zoff + t.y * TZ;
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
     const int m = P.step;
-    if (m > sd.nt) return;
     const Coef& cf = P.c;
     const int tile = t.y * g.ntx + t.x;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
@@ -983,6 +1002,8 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
 
     stage_tile(P.bcur + so, g, x0, z0, sm.sq);
     if (phys) stage_tile(P.pcur + so, g, x0, z0, sm.sp);
+    // only active shots are launched; the test comes after the copies are issued
+    if (m > sd.nt) { cp_async_wait(); return; }
 
     // adjoint sources r^m at the receivers when m-1 = k*jump
     const int rb = *GP(P.rtile + sd.rtile_off + tile), re = *GP(P.rtile + sd.rtile_off + tile + 1);
@@ -1097,9 +1118,11 @@ struct BwdIntSmem {
 // edge formula or strip), so the adjoint is L^T b = the staggered
 // differences with their signs exchanged, the rebuild is the interior
 // operator, and the imaging term is the rebuild's own stencil value.  The
-// per-cell operands (b^{m+2}, K, then p^m and g) are loaded before the
-// shared-memory phases that need them, so their latency overlaps the tile
-// staging and the x stages.
+// per-cell operands (b^{m+2}, K, then p^m and g) are loaded into registers
+// before the shared-memory phases that need them, so their latency overlaps
+// the tile staging and the x stages.  (Copying p^m and g into shared memory
+// at block start instead was 5% slower: 55 KB per block leaves too little of
+// the SM's shared memory and L1 for the concurrent general blocks.)
 __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
 {
     FWI_DYN_SMEM(smraw);
@@ -1109,7 +1132,6 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
     const int m = P.step;
-    if (m > sd.nt) return;
     const int txi = P.fast_tx0 + blockIdx.x, tzi = P.fast_tz0 + blockIdx.y;
     const int x0 = g.xoff + txi * TX, z0 = g.zoff + tzi * TZ;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
@@ -1131,6 +1153,8 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
         }
     stage_tile(P.bcur + so, g, x0, z0, sm.sq);
     stage_tile(P.pcur + so, g, x0, z0, sm.sp);
+    // only active shots are launched; the test comes after the loads are issued
+    if (m > sd.nt) { cp_async_wait(); return; }
 
     // adjoint sources r^m at the receivers when m-1 = k*jump
     const int tile = tzi * g.ntx + txi;
