@@ -273,6 +273,11 @@ constexpr bool kConcurrentClasses = true;
 
 cudaStream_t class_stream(const fwi_ctx* x, int cls) { return kConcurrentClasses ? x->side[cls] : x->st; }
 
+// Launch order of the general classes (0 = x-general, 1 = z-general, 2 =
+// corners): the z-general blocks are the most and run longest, so they start
+// first (2.5% shorter forward steps than x, z, corners on C2).
+constexpr int kClassOrder[3] = {1, 0, 2};
+
 // Forks the side streams of the non-empty classes from st.
 void fork_classes(fwi_ctx* x)
 {
@@ -304,7 +309,7 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
     P.shot_base = lo;
     fork_classes(x);
     const int2* gen = P.gen_tiles;
-    for (int cls = 0; cls < 3; ++cls) {
+    for (const int cls : kClassOrder) {
         const int cnt = x->gen_off[cls + 1] - x->gen_off[cls];
         if (!cnt) continue;
         P.gen_tiles = x->gen_d + x->gen_off[cls];
@@ -347,7 +352,7 @@ long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
     fork_classes(x);
     // z-only tiles never touch srx (the last member of BwdSmem)
     const int2* gen = P.gen_tiles;
-    for (int cls = 0; cls < 3; ++cls) {
+    for (const int cls : kClassOrder) {
         const int cnt = x->gen_off[cls + 1] - x->gen_off[cls];
         if (!cnt) continue;
         P.gen_tiles = x->gen_d + x->gen_off[cls];

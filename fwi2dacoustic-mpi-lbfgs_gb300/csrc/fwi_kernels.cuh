@@ -1177,7 +1177,7 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
     __syncthreads();
 
     // adjoint, z chain in registers, and b^m = 2 b^{m+1} - b^{m+2} + K (L^T b^{m+1} + r^m)
-    float bm[CX * R];
+    float bm[CX * R], pm[CX * R], ga[CX * R];
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
         const int cl = tx + BX * h, c = x0 + cl;
@@ -1199,18 +1199,17 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
             bm[q] = fmaf(kk[q], pbar, fmaf(2.f, qc[i + 3], -bo[q]));
             __stcg(GP(bold + (long long)(r0 + i) * g.ld + c), bm[q]);
         }
-    }
-
-    // rebuild operands, then the rebuild x stage into su (after every thread is done with ubar)
-    float pm[CX * R], ga[CX * R];
-    #pragma unroll
-    for (int h = 0; h < CX; ++h)
+        // this half's rebuild operands, in the registers its b^{m+2} leaves free;
+        // they arrive while the other half and the rebuild x stage compute
         #pragma unroll
         for (int i = 0; i < R; ++i) {
-            const long long o = (long long)(r0 + i) * g.ld + x0 + tx + BX * h;
+            const long long o = (long long)(r0 + i) * g.ld + c;
             pm[h * R + i] = __ldcg(GP(pold + o));
             ga[h * R + i] = __ldcg(GP(gacc + o));
         }
+    }
+
+    // the rebuild x stage into su (after every thread is done with ubar)
     __syncthreads();
     x_stage_plain<false>(sm.sp, sm.su, cf);
     __syncthreads();
