@@ -683,6 +683,12 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     c.c0x = fd[0]; c.c1x = fd[1]; c.ix = fd[2]; c.c0z = fd[3]; c.c1z = fd[4]; c.iz = fd[5];
     c.iz840 = fd[6]; c.iz24 = fd[7];
     c.iarea = 1.0 / (cfg->dx * cfg->dz);                    // fwi_2d.c:216
+    {   // D- D+ along x in one symmetric 7-point stencil (interior tiles)
+        const double a = c.c0x, b = c.c1x;
+        c.wx1 = (float)(a * a - 2.0 * a * b);
+        c.wx2 = (float)(2.0 * a * b);
+        c.wx3 = (float)(b * b);
+    }
 
     const int np = cfg->npml, n2 = 2 * np + 1;
     PsiLayout& pl = x->pl;

@@ -127,7 +127,27 @@ struct Geo {
 struct Coef {
     float c0x, c1x, ix, c0z, c1z, iz, iz840, iz24;   // fwi_2d.c:304-314
     float iarea;                                     // fwi_2d.c:216
+    float wx1, wx2, wx3;                             // dxx7 weights (from c0x, c1x)
 };
+
+// The x part of the plain operator, ux(c) = c0 (u(c+1) - u(c)) + c1 (u(c+2) -
+// u(c-1)) with u(j) = c0 (p[j] - p[j-1]) + c1 (p[j+1] - p[j-2])
+// (fwi_2d.c:775-784, 822-827), as one symmetric stencil of p[c-3 .. c+3]
+// with weights w1 = c0^2 - 2 c0 c1, w2 = 2 c0 c1, w3 = c1^2 for the
+// neighbours at distance 1, 2, 3 and -2 (w1 + w2 + w3) for the cell.  The
+// weights sum to zero, so it is evaluated on differences from the cell,
+// d_k = (p[c+k] - p[c]) + (p[c-k] - p[c]), which keeps the accuracy of the
+// two-stage form on smooth fields.  The adjoint x part of an interior tile
+// is the same stencil of b.  st[i] is the staged value at the cell.
+__device__ __forceinline__ float dxx7(const float* st, int i, const Coef& cf)
+{
+    [[maybe_unused]] constexpr int NS = SPH * SPW;
+    const float p0 = st[SIDX(i, NS)];
+    const float d1 = (st[SIDX(i + 1, NS)] - p0) + (st[SIDX(i - 1, NS)] - p0);
+    const float d2 = (st[SIDX(i + 2, NS)] - p0) + (st[SIDX(i - 2, NS)] - p0);
+    const float d3 = (st[SIDX(i + 3, NS)] - p0) + (st[SIDX(i - 3, NS)] - p0);
+    return cf.wx1 * d1 + cf.wx2 * d2 + cf.wx3 * d3;
+}
 
 // psi arrays of one shot, in the order u0,u1,v0,v1,ux0,ux1,vz0,vz1
 // (pml_profile, header.h:97; shapes fwi_2d.c:288-296).
@@ -614,41 +634,13 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_gen(const StepParams P)
     fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su);
 }
 
-// Plain x stage of an interior tile: u = c0 (p[j] - p[j-1]) + c1 (p[j+1] - p[j-2])
-// (ADJ false) or its transpose ubar = c0 (q[j-1] - q[j]) + c1 (q[j-2] - q[j+1])
-// (ADJ true) at the UW u positions j = x0 - 1 + jj of the TZ rows, from the
-// staged tile st into su.  Each warp computes the first 2 BX positions of its
-// rows with all lanes busy; the UW - 2 BX halo positions of all rows follow
-// in one pass spread over the block.
-template <bool ADJ>
-__device__ __forceinline__ void x_stage_plain(const float* st, float* su, const Coef& cf)
-{
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    [[maybe_unused]] constexpr int NS = SPH * SPW, NU = TZ * UWP;
-    constexpr int XH = UW - 2 * BX;
-    auto one = [&](int rl, int jj) {
-        const int q = (rl + HZ) * SPW + HX - 1 + jj;                      // st index of column j
-        float v;
-        if (!ADJ) v = cf.c0x * (st[SIDX(q, NS)] - st[SIDX(q - 1, NS)]) + cf.c1x * (st[SIDX(q + 1, NS)] - st[SIDX(q - 2, NS)]);
-        else      v = cf.c0x * (st[SIDX(q - 1, NS)] - st[SIDX(q, NS)]) + cf.c1x * (st[SIDX(q - 2, NS)] - st[SIDX(q + 1, NS)]);
-        su[SIDX(rl * UWP + jj, NU)] = v;
-    };
-    #pragma unroll
-    for (int k = 0; k < R; ++k) {
-        #pragma unroll
-        for (int h = 0; h < 2; ++h) one(ty + BY * k, tx + BX * h);
-    }
-    const int t = ty * BX + tx;
-    if (t < XH * TZ) one(t / XH, 2 * BX + t % XH);
-}
-
 // Forward step, interior tiles: no edge, CPML or strip cells, so every cell
-// takes the same branch-free stencil.  The per-cell loads of p^{it-1} and K
-// are issued before the tile copy so that their latencies overlap.
+// takes the same branch-free stencil, its x part as dxx7 of the staged tile.
+// The per-cell loads of p^{it-1} and K are issued before the tile copy so
+// that their latencies overlap.
 __global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
 {
     __shared__ __align__(16) float sp[SPH * SPW];
-    __shared__ __align__(16) float su[TZ * UWP];
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
     const Geo& g = P.g;
@@ -674,8 +666,6 @@ __global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
     if (P.step >= sd.nt) { cp_async_wait(); return; }
     cp_async_wait();
     __syncthreads();
-    x_stage_plain<false>(sp, su, cf);
-    __syncthreads();
     const float amp = *GP(P.wav + sd.wav_off + P.step) * cf.iarea;
     const bool src_tile = sd.src_r >= z0 && sd.src_r < z0 + TZ && sd.src_c >= x0 && sd.src_c < x0 + TX;   // uniform
     #pragma unroll
@@ -690,10 +680,8 @@ __global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i;
-            const int u0 = (r0l + i) * UWP + 1 + cl;                      // su index of u position c
             const float vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
-            const float ux = cf.c0x * (su[SIDX(u0 + 1, TZ * UWP)] - su[SIDX(u0, TZ * UWP)]) +
-                             cf.c1x * (su[SIDX(u0 + 2, TZ * UWP)] - su[SIDX(u0 - 1, TZ * UWP)]);
+            const float ux = dxx7(sp, (r0l + i + HZ) * SPW + HX + cl, cf);
             const float k1 = kk[h * R + i];
             float pn = fmaf(k1, ux + vz, fmaf(2.f, pc[i + 3], -po[h * R + i]));
             if (src_tile && row == sd.src_r && c == sd.src_c) pn += amp * k1;
@@ -1103,13 +1091,12 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
     }
 }
 
-// Shared memory of an interior backward tile: the adjoint x stage needs no
-// psi-adjusted copy (srx), so interior blocks are launched with this smaller
-// layout (sizeof(BwdIntSmem) dynamic bytes).
+// Shared memory of an interior backward tile: the x parts are dxx7 of the
+// staged tiles, so interior blocks need neither u positions nor a
+// psi-adjusted copy (sizeof(BwdIntSmem) dynamic bytes).
 struct BwdIntSmem {
     float sq[SPH * SPW];   // b^{m+1} tile + halo
     float sp[SPH * SPW];   // p^{m-1} tile + halo
-    float su[TZ * UWP];    // adjoint ubar, then rebuild u
     float racc[TZ * TX];   // receiver adjoint sources of the tile
 };
 
@@ -1118,12 +1105,13 @@ struct BwdIntSmem {
 // edge formula or strip), so the adjoint is L^T b = the staggered
 // differences with their signs exchanged, the rebuild is the interior
 // operator, and the imaging term is the rebuild's own stencil value.  The
-// per-cell operands (b^{m+2}, K, then p^m and g) are loaded into registers
-// before the shared-memory phases that need them, so their latency overlaps
-// the tile staging and the x stages.  (Copying p^m and g into shared memory
-// at block start instead was 5% slower: 55 KB per block leaves too little of
-// the SM's shared memory and L1 for the concurrent general blocks.)
-__global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
+// x parts are dxx7 of the staged tiles, so one barrier (after the tile
+// copies) is all the block needs.  Every per-cell operand (b^{m+2}, K, p^m,
+// g) is loaded into registers at block start, with the tile copies.
+// (Copying p^m and g into shared memory instead was 5% slower: 55 KB per
+// block leaves too little of the SM's shared memory and L1 for the
+// concurrent general blocks.)
+__global__ void __launch_bounds__(NTH, 4) k_bwd_int(const StepParams P)
 {
     FWI_DYN_SMEM(smraw);
     BwdIntSmem& sm = *reinterpret_cast<BwdIntSmem*>(smraw);
@@ -1140,9 +1128,9 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
     float* __restrict__ pold = P.pold + so;
     float* __restrict__ gacc = P.gacc + so;
     const int r0l = R * ty, r0 = z0 + r0l;
-    [[maybe_unused]] constexpr int NS = SPH * SPW, NU = TZ * UWP;
+    [[maybe_unused]] constexpr int NS = SPH * SPW;
 
-    float bo[CX * R], kk[CX * R];
+    float bo[CX * R], kk[CX * R], pm[CX * R], ga[CX * R];
     #pragma unroll
     for (int h = 0; h < CX; ++h)
         #pragma unroll
@@ -1150,6 +1138,8 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
             const long long o = (long long)(r0 + i) * g.ld + x0 + tx + BX * h;
             bo[h * R + i] = __ldcg(GP(bold + o));
             kk[h * R + i] = __ldg(GP(P.K + o));
+            pm[h * R + i] = __ldcg(GP(pold + o));
+            ga[h * R + i] = __ldcg(GP(gacc + o));
         }
     stage_tile(P.bcur + so, g, x0, z0, sm.sq);
     stage_tile(P.pcur + so, g, x0, z0, sm.sp);
@@ -1172,12 +1162,9 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
     cp_async_wait();
     __syncthreads();
 
-    // adjoint, x: ubar[j] = c0 (q[j-1] - q[j]) + c1 (q[j-2] - q[j+1]) at u positions j in [x0-1, x0+TX+1]
-    x_stage_plain<true>(sm.sq, sm.su, cf);
-    __syncthreads();
-
-    // adjoint, z chain in registers, and b^m = 2 b^{m+1} - b^{m+2} + K (L^T b^{m+1} + r^m)
-    float bm[CX * R], pm[CX * R], ga[CX * R];
+    // adjoint: the z chain in registers, the x part as dxx7 of b^{m+1} (the
+    // interior operator is symmetric), and b^m = 2 b^{m+1} - b^{m+2} + K (L^T b^{m+1} + r^m)
+    float bm[CX * R];
     #pragma unroll
     for (int h = 0; h < CX; ++h) {
         const int cl = tx + BX * h, c = x0 + cl;
@@ -1189,30 +1176,15 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
         for (int k = 0; k < R + 3; ++k) vb[k] = cf.c0z * (qc[k + 1] - qc[k + 2]) + cf.c1z * (qc[k] - qc[k + 3]);
         #pragma unroll
         for (int i = 0; i < R; ++i) {
-            const int u0 = (r0l + i) * UWP + 1 + cl;                  // su index of u position c
             const float pz = cf.c0z * (vb[i + 1] - vb[i + 2]) + cf.c1z * (vb[i] - vb[i + 3]);
-            const float px = cf.c0x * (sm.su[SIDX(u0, NU)] - sm.su[SIDX(u0 + 1, NU)]) +
-                             cf.c1x * (sm.su[SIDX(u0 - 1, NU)] - sm.su[SIDX(u0 + 2, NU)]);
+            const float px = dxx7(sm.sq, (r0l + i + HZ) * SPW + HX + cl, cf);
             float pbar = px + pz;
             if (do_res) pbar += sm.racc[SIDX((r0l + i) * TX + cl, TZ * TX)];
             const int q = h * R + i;
             bm[q] = fmaf(kk[q], pbar, fmaf(2.f, qc[i + 3], -bo[q]));
             __stcg(GP(bold + (long long)(r0 + i) * g.ld + c), bm[q]);
         }
-        // this half's rebuild operands, in the registers its b^{m+2} leaves free;
-        // they arrive while the other half and the rebuild x stage compute
-        #pragma unroll
-        for (int i = 0; i < R; ++i) {
-            const long long o = (long long)(r0 + i) * g.ld + c;
-            pm[h * R + i] = __ldcg(GP(pold + o));
-            ga[h * R + i] = __ldcg(GP(gacc + o));
-        }
     }
-
-    // the rebuild x stage into su (after every thread is done with ubar)
-    __syncthreads();
-    x_stage_plain<false>(sm.sp, sm.su, cf);
-    __syncthreads();
 
     // rebuild p^{m-2} = 2 p^{m-1} - p^m + K (L p^{m-1} + s^{m-1}) and imaging g += b^m (L p^{m-1} + f^{m-1})
     const float f = *GP(P.wav + sd.wav_off + m - 1) * cf.iarea;
@@ -1230,10 +1202,8 @@ __global__ void __launch_bounds__(NTH) k_bwd_int(const StepParams P)
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i, q = h * R + i;
             const long long o = (long long)row * g.ld + c;
-            const int u0 = (r0l + i) * UWP + 1 + cl;
             const float vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
-            const float ux = cf.c0x * (sm.su[SIDX(u0 + 1, NU)] - sm.su[SIDX(u0, NU)]) +
-                             cf.c1x * (sm.su[SIDX(u0 + 2, NU)] - sm.su[SIDX(u0 - 1, NU)]);
+            const float ux = dxx7(sm.sp, (r0l + i + HZ) * SPW + HX + cl, cf);
             float lp = ux + vz;
             float pn = fmaf(kk[q], lp, fmaf(2.f, pc[i + 3], -pm[q]));
             if (src_tile && row == sd.src_r && c == sd.src_c) { pn += f * kk[q]; lp += f; }
