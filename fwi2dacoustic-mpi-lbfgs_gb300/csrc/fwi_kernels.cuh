@@ -448,8 +448,10 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             }
         }
     }
+    // u positions into su: x-general tiles only (elsewhere the x part is dxx7 of sp)
     #pragma unroll
     for (int k = 0; k < R; ++k) {
+        if (!GX) break;
         const int rl = ty + BY * k, row = z0 + rl;
         if (GZ && (row < 0 || row >= g.pnz)) continue;                      // rows outside the grid
         const int pbase = (rl + HZ) * SPW + HX - x0;                       // + global column = sp index
@@ -479,7 +481,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             su[SIDX(rl * UWP + jj, TZ * UWP)] = u;
         }
     }
-    __syncthreads();
+    if (GX) __syncthreads();
 
     const float* __restrict__ K = P.K;
     float* __restrict__ pold = P.pold + so;
@@ -567,7 +569,9 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                     vz = 0.f;
                 }
             }
-            if (!gxc) {
+            if (!GX) {
+                ux = dxx7(sp, (r0l + i + HZ) * SPW + HX + cl, cf);
+            } else if (!gxc) {
                 ux = cf.c0x * (UR(c + 1) - UR(c)) + cf.c1x * (UR(c + 2) - UR(c - 1));
             } else {
                 if (c >= 1 && c <= g.pnx - 2) {
@@ -784,9 +788,11 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         }
         __syncthreads();
     }
-    // x stage 2: ubar at u positions j in [x0-1, x0+TX+1]
+    // x stage 2: ubar at u positions j in [x0-1, x0+TX+1], x-general tiles only
+    // (elsewhere the adjoint x part is dxx7 of sq)
     #pragma unroll
     for (int k = 0; k < R; ++k) {
+        if (!GX) break;
         const int rl = ty + BY * k, row = z0 + rl;
         if (GZ && (row < 0 || row >= pnz)) continue;
         #pragma unroll
@@ -822,7 +828,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             sm.su[SIDX(rl * UWP + jj, NU)] = ub;
         }
     }
-    __syncthreads();
+    if (GX) __syncthreads();
 
     const float* __restrict__ K = P.K;
     float* __restrict__ bold = P.bold + so;
@@ -939,7 +945,9 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 if (row == pnz - 1) pz += cf.iz * vb[i + 1];
                 if (row == pnz - 2) pz -= cf.iz * vb[i + 2];
             }
-            if (!gxc) {
+            if (!GX) {
+                px = dxx7(sm.sq, (r0l + i + HZ) * SPW + HX + cl, cf);
+            } else if (!gxc) {
                 px = cf.c0x * (UB(c) - UB(c + 1)) + cf.c1x * (UB(c - 1) - UB(c + 2));
             } else {
                 #define UM(j) (((j) >= 2 && (j) <= pnx - 2) ? UB(j) : 0.f)
@@ -1012,10 +1020,12 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
     adj_tile<GX, GZ>(P, sd, s, x0, z0, sm, do_res, bm);
     if (!phys) return;   // uniform per block
 
-    // rebuild of p^{m-2} and imaging (physical cells only)
-    __syncthreads();     // su is reused
+    // rebuild of p^{m-2} and imaging (physical cells only); the u positions
+    // of p^{m-1} into su for x-general tiles (elsewhere the x part is dxx7 of sp)
+    if (GX) __syncthreads();     // su is reused
     #pragma unroll
     for (int k = 0; k < R; ++k) {
+        if (!GX) break;
         const int rl = ty + BY * k;
         if (GZ && (z0 + rl < zp0 || z0 + rl >= zp1)) continue;
         #pragma unroll
@@ -1027,7 +1037,7 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
                                              cf.c1x * (sm.sp[SIDX(p0 + 1, NS)] - sm.sp[SIDX(p0 - 2, NS)]);
         }
     }
-    __syncthreads();
+    if (GX) __syncthreads();
     const float* __restrict__ K = P.K;
     float* __restrict__ pold = P.pold + so;
     float* __restrict__ gacc = P.gacc + so;
@@ -1075,8 +1085,9 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
             if (!strip) {
                 const int u0 = (r0l + i) * UWP + 1 + cl;        // su index of u position c
                 const float vz = cf.c0z * (vv[i + 2] - vv[i + 1]) + cf.c1z * (vv[i + 3] - vv[i]);
-                const float ux = cf.c0x * (sm.su[SIDX(u0 + 1, NU)] - sm.su[SIDX(u0, NU)]) +
-                                 cf.c1x * (sm.su[SIDX(u0 + 2, NU)] - sm.su[SIDX(u0 - 1, NU)]);
+                const float ux = GX ? cf.c0x * (sm.su[SIDX(u0 + 1, NU)] - sm.su[SIDX(u0, NU)]) +
+                                          cf.c1x * (sm.su[SIDX(u0 + 2, NU)] - sm.su[SIDX(u0 - 1, NU)])
+                                    : dxx7(sm.sp, (r0l + i + HZ) * SPW + HX + cl, cf);
                 const float w = ux + vz;
                 pn = fmaf(kk, w, fmaf(2.f, p1, -pm));
                 lp = w;
