@@ -33,6 +33,7 @@
 #define __host__
 #define __forceinline__ inline
 #define __launch_bounds__(...)
+#define __grid_constant__
 #define __shared__ static
 #define __align__(n) __attribute__((aligned(n)))
 #define FWI_DYN_SMEM(name) unsigned char* name = fwi_emu::dyn_smem()

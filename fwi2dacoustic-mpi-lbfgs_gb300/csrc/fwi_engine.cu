@@ -8,6 +8,9 @@
 #include "fwi_gb300.h"
 #include "fwi_kernels.cuh"
 #include "fwi_aux.cuh"
+#ifndef FWI_CPU_EMU
+#include <cudaTypedefs.h>
+#endif
 
 #include <algorithm>
 #include <cmath>
@@ -116,6 +119,8 @@ struct fwi_ctx {
     RecDev* recs_d = nullptr;      // receivers grouped by tile (backward injection)
     int* rtile_d = nullptr;        // per-slot, per-tile CSR of recs_d
     int2* gen_d = nullptr;         // tiles of the general path, grouped by class (GX only, GZ only, both)
+    int* err_d = nullptr;          // set by a kernel whose tile copy timed out (StepParams::err)
+    TensorMap tm_F[2], tm_A[2];    // TMA maps of the two halves of F (p) and A (b)
     int ngen = 0;
     int gen_off[4] = {};           // class c occupies gen_d[gen_off[c], gen_off[c + 1])
     int ftx0 = 0, ftx1 = 0, ftz0 = 0, ftz1 = 0;   // interior tile rectangle
@@ -214,6 +219,7 @@ StepParams base_params(const fwi_ctx* x)
     P.gen_arith = x->gen_arith;
     P.recs = x->recs_d;
     P.rtile = x->rtile_d;
+    P.err = x->err_d;
     P.wav = x->wav;
     P.syn = x->syn;
     P.res = x->res;
@@ -366,7 +372,7 @@ long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
     }
     P.gen_tiles = gen;
     if (x->ftx1 > x->ftx0 && x->ftz1 > x->ftz0) {
-        FWI_LAUNCH(k_bwd_int, dim3(x->ftx1 - x->ftx0, x->ftz1 - x->ftz0, n), block, sizeof(BwdIntSmem), x->st, P);
+        FWI_LAUNCH(k_bwd_int, dim3(x->ftx1 - x->ftx0, x->ftz1 - x->ftz0, n), block, BWD_INT_SMEM, x->st, P);
         DIAG_SYNC("k_bwd_int");
         ++l;
     }
@@ -391,6 +397,7 @@ int run_forward(fwi_ctx* x)
             const int hi = x->cfg.plain_per_shot ? grp + 1 : active_slots(x, it + 1);
             P.step = it;
             P.pcur = x->F + (long long)(it & 1) * half + x->origin;
+            P.tm_pcur = x->tm_F[it & 1];
             P.pold = x->F + (long long)((it + 1) & 1) * half + x->origin;
             P.psr = x->psiF + (long long)(it & 1) * phalf;
             P.psw = x->psiF + (long long)((it + 1) & 1) * phalf;
@@ -448,8 +455,10 @@ int run_backward(fwi_ctx* x)
             const int hi = x->cfg.plain_per_shot ? grp + 1 : active_slots(x, m);
             P.step = m;
             P.pcur = x->F + (long long)((m - 1) & 1) * half + x->origin;   // p^{m-1}
+            P.tm_pcur = x->tm_F[(m - 1) & 1];
             P.pold = x->F + (long long)(m & 1) * half + x->origin;         // p^m -> p^{m-2}
             P.bcur = x->A + (long long)((m + 1) & 1) * half + x->origin;   // b^{m+1}
+            P.tm_bcur = x->tm_A[(m + 1) & 1];
             P.bold = x->A + (long long)(m & 1) * half + x->origin;         // b^{m+2} -> b^m
             P.psr = x->psiA + (long long)(m & 1) * phalf;
             P.psw = x->psiA + (long long)((m + 1) & 1) * phalf;
@@ -474,7 +483,48 @@ float event_ms(cudaEvent_t a, cudaEvent_t b)
 int finish(fwi_ctx* x)
 {
     CK(cudaStreamSynchronize(x->st));
+    int bad = 0;
+    CK(cudaMemcpy(&bad, x->err_d, sizeof(int), cudaMemcpyDeviceToHost));
+    if (bad) {
+        cudaMemset(x->err_d, 0, sizeof(int));
+        return fail(x, FWI_ERR_CUDA, "a tile copy (TMA) did not complete within its bounded wait");
+    }
     return FWI_OK;
+}
+
+// The TMA map of one field half (base: its first float): dims (ld, rows,
+// slots) of floats with the fields' strides, box SPW x SPH x 1, no swizzle,
+// zero fill outside.  cuTensorMapEncodeTiled comes through the runtime's
+// driver entry point, so the library links no driver library.
+int encode_field_map(TensorMap* out, float* base, const Geo& g, int rows, int slots)
+{
+#ifdef FWI_CPU_EMU
+    (void)base; (void)g; (void)rows; (void)slots;
+    *out = TensorMap{};
+    return 0;
+#else
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !f)
+            return -1;
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }
+    static_assert(sizeof(CUtensorMap) == sizeof(TensorMap), "a TensorMap holds one CUtensorMap");
+    CUtensorMap m;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.ld, (cuuint64_t)rows, (cuuint64_t)slots};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.ld * sizeof(float), (cuuint64_t)g.fstride * sizeof(float)};
+    const cuuint32_t box[3] = {(cuuint32_t)SPW, (cuuint32_t)SPH, 1};
+    const cuuint32_t unit[3] = {1, 1, 1};
+    if (encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+        CUDA_SUCCESS)
+        return -1;
+    std::memcpy(out, &m, sizeof m);
+    return 0;
+#endif
 }
 
 enum Phase { PH_FWD = 0, PH_MIS = 1, PH_BWD = 2 };
@@ -673,6 +723,8 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
         x->ftx0 = tx0; x->ftx1 = tx1; x->ftz0 = tz0; x->ftz1 = tz1;
         x->ngen = (int)gen.size();
         if (dalloc(x, &x->gen_d, gen.size(), &x->bytes_model)) return bail(FWI_ERR_NOMEM);
+        if (dalloc(x, &x->err_d, 1, &x->bytes_model) || cudaMemset(x->err_d, 0, sizeof(int)) != cudaSuccess)
+            return bail(FWI_ERR_NOMEM);
         if (!gen.empty() && cudaMemcpy(x->gen_d, gen.data(), gen.size() * sizeof(int2), cudaMemcpyHostToDevice) != cudaSuccess)
             return bail(FWI_ERR_CUDA);
     }
@@ -724,7 +776,7 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     if (cudaMemsetAsync(x->K, 0, sizeof(float) * g.fstride, x->st) != cudaSuccess ||
         cudaStreamSynchronize(x->st) != cudaSuccess)
         return bail(FWI_ERR_CUDA);
-    if (cudaFuncSetAttribute(k_bwd_int, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BwdIntSmem)) !=
+    if (cudaFuncSetAttribute(k_bwd_int, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BWD_INT_SMEM) !=
             cudaSuccess ||
         cudaFuncSetAttribute(k_bwd_edge<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(BwdSmem)) != cudaSuccess ||
@@ -741,7 +793,7 @@ void fwi_destroy(fwi_ctx* x)
 {
     if (!x) return;
     free_shots(x);
-    void* ps[] = {x->K, x->vel, x->pmlc, x->grad, x->gradf, x->gen_d};
+    void* ps[] = {x->K, x->vel, x->pmlc, x->grad, x->gradf, x->gen_d, x->err_d};
     for (void* p : ps) if (p) cudaFree(p);
     for (auto& e : x->ev) if (e) cudaEventDestroy(e);
     for (auto& e : x->join_ev) if (e) cudaEventDestroy(e);
@@ -903,6 +955,12 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     e = e ? e : dalloc(x, &x->geo_d, geo.size(), &b);
     e = e ? e : dalloc(x, &x->xpart_d, geo.size(), &b);
     if (e) { std::string m = x->err; free_shots(x); x->err = m; return e; }
+    for (int h = 0; h < 2; ++h)
+        if (encode_field_map(&x->tm_F[h], x->F + h * half, g, x->rows_alloc, nshots) ||
+            encode_field_map(&x->tm_A[h], x->A + h * half, g, x->rows_alloc, nshots)) {
+            free_shots(x);
+            return fail(x, FWI_ERR_CUDA, "cuTensorMapEncodeTiled failed for a field");
+        }
     CK(cudaMemcpyAsync(x->shots_d, slot.data(), sizeof(ShotDev) * nshots, cudaMemcpyHostToDevice, x->st));
     if (!samp.empty()) {
         CK(cudaMemcpyAsync(x->samp_d, samp.data(), sizeof(RecSample) * samp.size(), cudaMemcpyHostToDevice, x->st));

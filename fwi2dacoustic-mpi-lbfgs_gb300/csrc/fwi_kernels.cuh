@@ -193,6 +193,12 @@ struct RecParams {
     int step, jump;
 };
 
+// A CUtensorMap (128 bytes, 64-byte aligned) encoded on the host for one
+// field half: dims (ld, rows_alloc, shots) of floats, box SPW x SPH x 1.
+struct alignas(64) TensorMap {
+    unsigned long long w[16];
+};
+
 struct StepParams {
     Geo g;
     Coef c;
@@ -221,6 +227,9 @@ struct StepParams {
     int step;                // forward: it; backward: m
     int jump;
     int shot_base;           // slot of blockIdx.z == 0 (non-zero only when shots run one by one)
+    int* err;                // set to 1 by a block whose tile copy did not complete (bounded wait)
+    TensorMap tm_pcur;       // pcur's field half (interior tiles stage it with TMA)
+    TensorMap tm_bcur;       // bcur's field half (backward)
 };
 
 // A tile takes the general path when its cells or their stencil halo touch a
@@ -368,6 +377,51 @@ __device__ __forceinline__ void cp_async_wait()
     asm volatile("cp.async.wait_all;\n" ::: "memory");
 #endif
 }
+
+// Tensor-memory-access (TMA) copies of staged tiles: one thread arms an
+// mbarrier with the expected bytes and issues cp.async.bulk.tensor; every
+// thread waits on the barrier's phase 0.  The wait is bounded: a block whose
+// copy has not landed after TMA_SPINS polls sets *err and skips its tile,
+// and the host reports the error.  Tile destinations are 128-byte aligned;
+// the x coordinate x0 - xoff is a multiple of 64 floats.
+constexpr int TMA_SPINS = 1 << 22;
+constexpr unsigned TILE_BYTES = SPH * SPW * sizeof(float);
+#ifndef FWI_CPU_EMU
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait0(unsigned long long* bar)
+{
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok) : "r"(smem_u32(bar)) : "memory");
+    return ok != 0;
+}
+// The tile of the field half tm whose interior starts at (z0, x0), shot s.
+__device__ __forceinline__ void tma_tile(float* dst, const TensorMap* tm, const Geo& g, int x0, int z0, int s,
+                                         unsigned long long* bar)
+{
+    const int x = x0 - g.xoff, y = z0 - g.zoff + MZ - HZ;             // allocation column and row of the box
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4}], [%5];\n"
+                 ::"r"(smem_u32(dst)), "l"(tm), "r"(x), "r"(y), "r"(s), "r"(smem_u32(bar)) : "memory");
+}
+// Bounded wait for phase 0; false (and *err set) when it did not complete.
+__device__ __forceinline__ bool tma_wait(unsigned long long* bar, int* err)
+{
+    for (int i = 0; i < TMA_SPINS; ++i)
+        if (mbar_try_wait0(bar)) return true;
+    atomicExch(err, 1);
+    return false;
+}
+#endif
 
 // Starts copying the (TZ+2HZ) x (TX+2HX) tile of field f whose interior
 // starts at (z0, x0) into shared memory in 16-byte pieces; cp_async_wait()
@@ -642,9 +696,10 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_gen(const StepParams P)
 // takes the same branch-free stencil, its x part as dxx7 of the staged tile.
 // The per-cell loads of p^{it-1} and K are issued before the tile copy so
 // that their latencies overlap.
-__global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
+__global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const __grid_constant__ StepParams P)
 {
-    __shared__ __align__(16) float sp[SPH * SPW];
+    __shared__ __align__(128) float sp[SPH * SPW];
+    __shared__ __align__(8) unsigned long long bar;
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
     const Geo& g = P.g;
@@ -657,6 +712,14 @@ __global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
     const long long o0 = (long long)r0 * g.ld + x0 + tx;
     float* __restrict__ prow = P.pold + so + o0;
     const float* __restrict__ krow = P.K + o0;
+#ifndef FWI_CPU_EMU
+    if (ty == 0 && tx == 0) mbar_init(&bar);
+    __syncthreads();
+    if (ty == 0 && tx == 0) {                             // the tile of p^it, one TMA copy
+        mbar_expect_tx(&bar, TILE_BYTES);
+        tma_tile(sp, &P.tm_pcur, g, x0, z0, s, &bar);
+    }
+#endif
     float po[CX * R], kk[CX * R];
     #pragma unroll
     for (int h = 0; h < CX; ++h)
@@ -665,11 +728,15 @@ __global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const StepParams P)
             po[h * R + i] = __ldcg(GP(prow + i * g.ld + BX * h));
             kk[h * R + i] = __ldg(GP(krow + i * g.ld + BX * h));
         }
+#ifdef FWI_CPU_EMU
     stage_tile(P.pcur + so, g, x0, z0, sp);
-    // only active shots are launched; the test comes after the loads are issued
-    if (P.step >= sd.nt) { cp_async_wait(); return; }
-    cp_async_wait();
     __syncthreads();
+    if (P.step >= sd.nt) return;
+#else
+    // the block leaves only after its copy has landed (or timed out, uniformly);
+    // only active shots are launched, so the shot test never fires
+    if (__syncthreads_or(!tma_wait(&bar, P.err)) || P.step >= sd.nt) return;
+#endif
     const float amp = *GP(P.wav + sd.wav_off + P.step) * cf.iarea;
     const bool src_tile = sd.src_r >= z0 && sd.src_r < z0 + TZ && sd.src_c >= x0 && sd.src_c < x0 + TX;   // uniform
     #pragma unroll
@@ -1105,11 +1172,15 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
 // Shared memory of an interior backward tile: the x parts are dxx7 of the
 // staged tiles, so interior blocks need neither u positions nor a
 // psi-adjusted copy (sizeof(BwdIntSmem) dynamic bytes).
+constexpr int SPA = (SPH * SPW + 31) / 32 * 32;   // staged tile padded to 128 bytes
 struct BwdIntSmem {
-    float sq[SPH * SPW];   // b^{m+1} tile + halo
-    float sp[SPH * SPW];   // p^{m-1} tile + halo
+    float sq[SPA];         // b^{m+1} tile + halo (TMA destination, 128-byte aligned)
+    float sp[SPA];         // p^{m-1} tile + halo
     float racc[TZ * TX];   // receiver adjoint sources of the tile
+    unsigned long long bar;   // mbarrier of the two tile copies
 };
+// Launch size of k_bwd_int: the layout plus room to align it to 128 bytes.
+constexpr size_t BWD_INT_SMEM = sizeof(BwdIntSmem) + 128;
 
 // Backward step, interior tiles (the rectangle fast_tx0.. x fast_tz0..):
 // every cell and stencil neighbour is a physical interior cell (no CPML,
@@ -1124,10 +1195,14 @@ struct BwdIntSmem {
 // (Copying p^m and g into shared memory instead was 5% slower: 55 KB per
 // block leaves too little of the SM's shared memory and L1 for the
 // concurrent general blocks.)
-__global__ void __launch_bounds__(NTH, 4) k_bwd_int(const StepParams P)
+__global__ void __launch_bounds__(NTH, 4) k_bwd_int(const __grid_constant__ StepParams P)
 {
     FWI_DYN_SMEM(smraw);
+#ifdef FWI_CPU_EMU
     BwdIntSmem& sm = *reinterpret_cast<BwdIntSmem*>(smraw);
+#else
+    BwdIntSmem& sm = *reinterpret_cast<BwdIntSmem*>(smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u));
+#endif
     const Geo& g = P.g;
     const Coef& cf = P.c;
     const int s = blockIdx.z + P.shot_base;
@@ -1143,6 +1218,15 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_int(const StepParams P)
     const int r0l = R * ty, r0 = z0 + r0l;
     [[maybe_unused]] constexpr int NS = SPH * SPW;
 
+#ifndef FWI_CPU_EMU
+    if (tid == 0) mbar_init(&sm.bar);
+    __syncthreads();
+    if (tid == 0) {                                       // the tiles of b^{m+1} and p^{m-1}, two TMA copies
+        mbar_expect_tx(&sm.bar, 2 * TILE_BYTES);
+        tma_tile(sm.sq, &P.tm_bcur, g, x0, z0, s, &sm.bar);
+        tma_tile(sm.sp, &P.tm_pcur, g, x0, z0, s, &sm.bar);
+    }
+#endif
     float bo[CX * R], kk[CX * R], pm[CX * R], ga[CX * R];
     #pragma unroll
     for (int h = 0; h < CX; ++h)
@@ -1152,10 +1236,15 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_int(const StepParams P)
             bo[h * R + i] = __ldcg(GP(bold + o));
             kk[h * R + i] = __ldg(GP(P.K + o));
         }
+#ifdef FWI_CPU_EMU
     stage_tile(P.bcur + so, g, x0, z0, sm.sq);
     stage_tile(P.pcur + so, g, x0, z0, sm.sp);
+    if (m > sd.nt) return;
+#else
     // only active shots are launched; the test comes after the loads are issued
-    if (m > sd.nt) { cp_async_wait(); return; }
+    // (a block leaves only after its copies have landed)
+    if (m > sd.nt) { __syncthreads_or(!tma_wait(&sm.bar, P.err)); return; }
+#endif
 
     // adjoint sources r^m at the receivers when m-1 = k*jump
     const int tile = tzi * g.ntx + txi;
@@ -1170,8 +1259,11 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_int(const StepParams P)
             atomicAdd(&sm.racc[SIDX(rd.cell, TZ * TX)], *GP(P.res + rd.syn_base + k));
         }
     }
-    cp_async_wait();
+#ifdef FWI_CPU_EMU
     __syncthreads();
+#else
+    if (__syncthreads_or(!tma_wait(&sm.bar, P.err))) return;   // uniform: every thread saw the same barrier
+#endif
 
     // adjoint: the z chain in registers, the x part as dxx7 of b^{m+1} (the
     // interior operator is symmetric), and b^m = 2 b^{m+1} - b^{m+2} + K (L^T b^{m+1} + r^m)
