@@ -381,10 +381,11 @@ __device__ __forceinline__ void cp_async_wait()
 // Tensor-memory-access (TMA) copies of staged tiles: one thread arms an
 // mbarrier with the expected bytes and issues cp.async.bulk.tensor; every
 // thread waits on the barrier's phase 0.  The wait is bounded: a block whose
-// copy has not landed after TMA_SPINS polls sets *err and skips its tile,
-// and the host reports the error.  Tile destinations are 128-byte aligned;
-// the x coordinate x0 - xoff is a multiple of 64 floats.
-constexpr int TMA_SPINS = 1 << 22;
+// copy has not landed after TMA_WAIT_CYCLES (about half a second), or that
+// finds the flag already raised by another block, sets *err and skips its
+// tile, and the host reports the error.  Tile destinations are 128-byte
+// aligned; the x coordinate x0 - xoff is a multiple of 64 floats.
+constexpr long long TMA_WAIT_CYCLES = 1LL << 30;
 constexpr unsigned TILE_BYTES = SPH * SPW * sizeof(float);
 #ifndef FWI_CPU_EMU
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -416,8 +417,11 @@ __device__ __forceinline__ void tma_tile(float* dst, const TensorMap* tm, const 
 // Bounded wait for phase 0; false (and *err set) when it did not complete.
 __device__ __forceinline__ bool tma_wait(unsigned long long* bar, int* err)
 {
-    for (int i = 0; i < TMA_SPINS; ++i)
+    const long long t0 = clock64();
+    for (unsigned i = 1;; ++i) {
         if (mbar_try_wait0(bar)) return true;
+        if ((i & 1023u) == 0 && (clock64() - t0 > TMA_WAIT_CYCLES || *(volatile int*)err)) break;
+    }
     atomicExch(err, 1);
     return false;
 }
