@@ -86,6 +86,10 @@ struct fwi_ctx {
     // graph keeps them as parallel branches.
     cudaStream_t side[3]{};
     cudaEvent_t fork_ev = nullptr, join_ev[3]{};
+    cudaStream_t samp_st = nullptr;                // receiver sampling, off the forward's critical path
+    cudaEvent_t step_ev = nullptr, samp_ev[2]{}, samp_done = nullptr;
+    bool samp_pending[2] = {false, false};         // a sample of that step parity is not yet waited for
+    bool samp_used = false;                        // samp_st has work in this forward pass
     cudaGraph_t graph[3]{};        // captured phases (use_graph): forward, misfit, backward
     cudaGraphExec_t gexec[3]{};
     long long graph_launches[3]{};
@@ -278,6 +282,9 @@ constexpr bool kConcurrentClasses = true;
 #endif
 
 cudaStream_t class_stream(const fwi_ctx* x, int cls) { return kConcurrentClasses ? x->side[cls] : x->st; }
+// Receiver sampling of step it reads p^{it+1}, which step it+2 overwrites
+// first: it runs on its own stream after step it, and step it+2 waits for it.
+constexpr bool kSampleAside = kConcurrentClasses;
 
 // Launch order of the general classes (0 = x-general, 1 = z-general, 2 =
 // corners): the z-general blocks are the most and run longest, so they start
@@ -313,6 +320,10 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
     const int n = hi - lo;
     long long l = 0;
     P.shot_base = lo;
+    if (x->samp_pending[P.step & 1]) {                 // the sample of step it-2 read the field this step writes
+        cudaStreamWaitEvent(x->st, x->samp_ev[P.step & 1], 0);
+        x->samp_pending[P.step & 1] = false;
+    }
     fork_classes(x);
     const int2* gen = P.gen_tiles;
     for (const int cls : kClassOrder) {
@@ -339,8 +350,19 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
         Q.lo = x->samp_off[lo];
         Q.hi = x->samp_off[hi];
         if (Q.hi > Q.lo) {
-            FWI_LAUNCH(k_sample, (Q.hi - Q.lo + 255) / 256, 256, 0, x->st, Q);
+            cudaStream_t ss = x->st;
+            if (kSampleAside) {
+                cudaEventRecord(x->step_ev, x->st);
+                cudaStreamWaitEvent(x->samp_st, x->step_ev, 0);
+                ss = x->samp_st;
+            }
+            FWI_LAUNCH(k_sample, (Q.hi - Q.lo + 255) / 256, 256, 0, ss, Q);
             DIAG_SYNC("k_sample");
+            if (kSampleAside) {
+                cudaEventRecord(x->samp_ev[P.step & 1], x->samp_st);
+                x->samp_pending[P.step & 1] = true;
+                x->samp_used = true;
+            }
             ++l;
         }
     }
@@ -404,6 +426,12 @@ int run_forward(fwi_ctx* x)
             launches += launch_fwd_step(x, P, lo, hi);
         }
     }
+    if (x->samp_used) {                                   // every sample lands before the misfit reads syn
+        cudaEventRecord(x->samp_done, x->samp_st);
+        cudaStreamWaitEvent(x->st, x->samp_done, 0);
+    }
+    x->samp_pending[0] = x->samp_pending[1] = false;
+    x->samp_used = false;
     CK(cudaGetLastError());
     x->stats.launches = launches;
     return FWI_OK;
@@ -664,6 +692,12 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
             cudaEventCreateWithFlags(&x->join_ev[i], cudaEventDisableTiming) != cudaSuccess)
             return bail(FWI_ERR_CUDA);
     if (cudaEventCreateWithFlags(&x->fork_ev, cudaEventDisableTiming) != cudaSuccess) return bail(FWI_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&x->samp_st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->step_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->samp_ev[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->samp_ev[1], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->samp_done, cudaEventDisableTiming) != cudaSuccess)
+        return bail(FWI_ERR_CUDA);
 
     Geo& g = x->g;
     g.nx = cfg->nx; g.nz = cfg->nz; g.npml = cfg->npml; g.fs = cfg->free_surface;
@@ -798,6 +832,8 @@ void fwi_destroy(fwi_ctx* x)
     for (auto& e : x->ev) if (e) cudaEventDestroy(e);
     for (auto& e : x->join_ev) if (e) cudaEventDestroy(e);
     if (x->fork_ev) cudaEventDestroy(x->fork_ev);
+    for (cudaEvent_t e : {x->step_ev, x->samp_ev[0], x->samp_ev[1], x->samp_done}) if (e) cudaEventDestroy(e);
+    if (x->samp_st) cudaStreamDestroy(x->samp_st);
     for (auto& t : x->side) if (t) cudaStreamDestroy(t);
     if (x->own) cudaStreamDestroy(x->own);
     delete x;
