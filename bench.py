@@ -15,13 +15,17 @@ imaging, and the FP64 reduction over shots.  Prints one JSON line.
   the misfit and the FP64 gradient.
 * ``roofline``: the dominant kernel (the fused backward step) at its
   algorithmic 36 B per physical cell-step against the measured HBM copy peak.
-* ``cpu_baseline``: the CPU port of the reference path (oracle/, all host
-  cores) on a bounded sample of the same workload, extrapolated; the same
-  sample checks the GPU gradient against the FP64 oracle.
+* ``cpu_baseline``: the reference's CPU path on the machine's host cores on a
+  bounded sample of the same workload (--cpu-shots shots, the first
+  --cpu-steps time steps), scaled linearly; ``kind`` "reference" when the reference's own
+  kernels are built (oracle/_ref: a_lap_opt_2d_pml, a_lap_opt_2d,
+  time_integral, write_bdr, read_bdr under a restated gradient driver, since
+  the reference's driver does not exist), else "port" (the restatement in
+  oracle/).  The first shot of the sample checks the GPU gradient against the
+  FP64 oracle.
 
-``--impl reference`` times only the CPU path (the reference's own algorithm,
-restated in oracle/ because the reference's gradient driver does not exist
-and its sources are not on the GPU host) on the same workload and metric.
+``--impl reference`` times only that CPU path, with all host threads, on the
+same workload and metric; it loads nothing but oracle/ libraries.
 """
 from __future__ import annotations
 
@@ -55,10 +59,16 @@ def parse():
     ap.add_argument("--nshots", type=int, default=None)
     ap.add_argument("--nt", type=int, default=None)
     ap.add_argument("--plain-shots", type=int, default=4)
-    ap.add_argument("--cpu-steps", type=int, default=4000, help="time steps of the CPU sample (at most the record)")
+    ap.add_argument("--cpu-steps", type=int, default=4000, help="time steps of the cpu_baseline sample and accuracy check")
     ap.add_argument("--cpu-shots", type=int, default=2, help="shots of the CPU sample in the cpu_baseline leg")
+    ap.add_argument("--ref-steps", type=int, default=500, help="time steps of each reference-arm sample")
     ap.add_argument("--no-graph", action="store_true")
-    ap.add_argument("--skip", default="", help="comma list of: e2e,plain,cpu")
+    ap.add_argument("--store", default="auto", choices=["auto", "strips", "snapshots"],
+                    help="forward-field storage of the backward half")
+    ap.add_argument("--snapshots", type=int, default=0, help="segments of the checkpointed backward (0: sqrt(nt))")
+    ap.add_argument("--snap-precision", default="f32", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--hbm-budget-mb", type=int, default=0, help="budget of --store auto (0: 90%% of free memory)")
+    ap.add_argument("--skip", default="", help="comma list of: e2e,plain,cpu,strips")
     return ap.parse_args()
 
 
@@ -141,88 +151,132 @@ def workload(args, world=1, rank=0):
     return cfgkw, vtrue, vstart, shots
 
 
-def describe(args, cfgkw, shots):
+STORE_NAMES = {0: "auto", 1: "strips", 2: "snapshots"}
+
+
+def describe(args, cfgkw, shots, stats=None):
     nts = sorted({s.nt for s in shots})
     nrs = sorted({s.nr for s in shots})
+    if stats is None or stats.get("store") in (None, 0, 1):
+        ckpt = "boundary strips of every step in HBM"
+    else:
+        ckpt = (f"checkpoints: {stats['segments']} segments, {args.snap_precision} storage, forward recompute "
+                f"per segment")
     return {"workload": f"{args.workload}: {cfgkw['nz']}x{cfgkw['nx']} grid, dx {cfgkw['dx']} m, "
                         f"dt {cfgkw['dt'] * 1e3:g} ms, CPML {cfgkw['npml']}, {len(shots)} shots",
             "nz": cfgkw["nz"], "nx": cfgkw["nx"], "npml": cfgkw["npml"], "shots": len(shots),
             "nt": nts[0] if len(nts) == 1 else [nts[0], nts[-1]],
             "receivers": nrs[0] if len(nrs) == 1 else [nrs[0], nrs[-1]],
-            "fd_order": 4, "free_surface": True, "checkpointing": "boundary strips in HBM",
+            "fd_order": 4, "free_surface": True, "checkpointing": ckpt,
+            "store_gb": None if stats is None else stats["store_bytes"] / 1e9,
             "l2": "working set larger than L2 (no flush)", "parallelism": f"shots batched per launch",
             "data": "synthetic seeded model and acquisition; observed traces modelled on the true model"}
 
 
-def cpu_sample(args, cfgkw, vstart, vtrue, shots, check_gpu=None, cache=None):
-    """Times the CPU port (oracle/, FP32, all host cores) on one gradient of
-    the given shots over the first args.cpu_steps time steps of the first
-    shot's record; optionally checks a GPU gradient of the first shot against
-    the FP64 oracle.  `cache` keeps the modelled observed traces between
-    calls."""
+def oracle_shots(O, o, shots, dx, dz, nt):
+    """The shots in cell indices for the CPU paths (the cell rounding of
+    fwi_2d.c:363-364, restated in the oracle), wavelets cut to nt steps."""
+    import numpy as np
+    out = []
+    for shot in shots:
+        isx, isz = o.cell_of(shot.src_x, shot.src_z, dx, dz)
+        cells = [o.cell_of(float(x), float(z), dx, dz) for x, z in shot.rec_xz]
+        irx = np.array([c[0] for c in cells], np.int32)
+        irz = np.array([c[1] for c in cells], np.int32)
+        out.append(O.Shot(isx, isz, irx, irz, shot.wavelet[:nt]))
+    return out
+
+
+def cpu_sample(args, cfgkw, vstart, vtrue, shots, nt_sample, kind, check_gpu=None, cache=None):
+    """Times one CPU gradient of the given shots over the first nt_sample
+    time steps of the first shot's record on all host cores: the reference's
+    own kernels driven as the reference would (kind "reference", oracle/_ref)
+    or the CPU restatement (kind "port", FP32 oracle).  Optionally checks a
+    GPU gradient of the first shot against the FP64 oracle.  `cache` keeps
+    the modelled observed traces between calls (setup, untimed)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle as O
-    import build as engine_build
     O.build()
-    engine_build.build()        # host helpers of the engine library (cell rounding)
     cache = {} if cache is None else cache
-    nt = min([args.cpu_steps] + [s.nt for s in shots])
+    nt = min([nt_sample] + [s.nt for s in shots])
     nt = (nt - 1) // cfgkw["jump"] * cfgkw["jump"] + 1
     cores = os.cpu_count() or 1
     ocfg = O.make_config(nx=cfgkw["nx"], nz=cfgkw["nz"], npml=cfgkw["npml"], nt=nt, dx=cfgkw["dx"],
                          dz=cfgkw["dz"], dt=cfgkw["dt"], free_surface=1, jump=cfgkw["jump"], nthreads=cores)
-    import fwigpu
-    dx, dz = cfgkw["dx"], cfgkw["dz"]
     o32 = O.Oracle("f32")
-    oshots, obss = [], []
-    for shot in shots:
-        isx, isz = fwigpu.cell_of(shot.src_x, shot.src_z, dx, dz)     # fwi_2d.c:363-364 rounding
-        cells = [fwigpu.cell_of(float(x), float(z), dx, dz) for x, z in shot.rec_xz]
-        irx = np.array([c[0] for c in cells], np.int32)
-        irz = np.array([c[1] for c in cells], np.int32)
-        osh = O.Shot(isx, isz, irx, irz, shot.wavelet[:nt])
+    oshots = oracle_shots(O, o32, shots, cfgkw["dx"], cfgkw["dz"], nt)
+    obss = []
+    for shot, osh in zip(shots, oshots):
         key = (id(shot), nt)
         if key not in cache:
             cache[key] = o32.forward(ocfg, vtrue, osh).astype(np.float32)
-        oshots.append(osh)
         obss.append(cache[key])
-    t0 = time.perf_counter()
-    J32, g32, _ = o32.gradient(ocfg, vstart, oshots, obss)
-    sec = time.perf_counter() - t0
-    out = {"sec": sec, "nt": nt, "shots": len(shots), "cores": cores}
+    if kind == "reference":
+        ref = O.RefKernels()
+        t0 = time.perf_counter()
+        ref.gradient(ocfg, vstart, oshots, obss)
+        sec = time.perf_counter() - t0
+    else:
+        t0 = time.perf_counter()
+        o32.gradient(ocfg, vstart, oshots, obss)
+        sec = time.perf_counter() - t0
+    out = {"sec": sec, "nt": nt, "shots": len(shots), "cores": cores, "kind": kind}
     if check_gpu is not None:
         o64 = O.Oracle("f64")
         J64, g64, _ = o64.gradient(ocfg, vstart, oshots[:1], obss[:1])
-        if len(shots) > 1:
-            J32, g32, _ = o32.gradient(ocfg, vstart, oshots[:1], obss[:1])
+        J32, g32, _ = o32.gradient(ocfg, vstart, oshots[:1], obss[:1])
         g_gpu = check_gpu(nt, obss[0])
         out["grad_rel_err"] = float(np.linalg.norm(g_gpu - g64) / np.linalg.norm(g64))
         out["grad_rel_err_cpu_fp32"] = float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))
     return out
 
 
+def cpu_kind():
+    """"reference" when the reference's own kernels are built (oracle/_ref),
+    else "port" (the oracle's restatement)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    return "reference" if O.RefKernels.available() else "port"
+
+
 def run_reference(args):
+    """The reference's CPU path on the workload: each timed step is one
+    gradient of one shot over the first --ref-steps time steps (a bounded
+    sample, 10-30 s of CPU work), and ms_per_step scales it linearly to the
+    full gradient of every shot of the workload."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     cfgkw, vtrue, vstart, shots = workload(args)
     nshots = len(shots)
+    kind = cpu_kind()
     times, cache = [], {}
-    for i in range(args.warmup + args.steps):
-        r = cpu_sample(args, cfgkw, vstart, vtrue, shots[:1], cache=cache)
-        if i >= args.warmup:
+    warm = max(3, args.warmup)
+    for i in range(warm + args.steps):
+        r = cpu_sample(args, cfgkw, vstart, vtrue, shots[:1], args.ref_steps, kind, cache=cache)
+        if i >= warm:
             times.append(r["sec"])
-    sec_shot = statistics.median(times) * shots[0].nt / r["nt"]         # linear in steps
-    ms_step = sec_shot * nshots * 1e3
+    sample_s = statistics.median(times)
+    factor = sum(s.nt for s in shots) / r["nt"]                 # linear in shot-steps
+    ms_step = sample_s * factor * 1e3
     value = nshots / (ms_step / 1e3)
-    sample = (f"1 shot of the workload, {r['nt']} of {shots[0].nt} steps (forward, misfit, adjoint, "
-              f"rebuild, imaging; FP32), scaled to {nshots} full shots")
+    what = ("the reference's own compiled kernels (a_lap_opt_2d_pml, a_lap_opt_2d, time_integral, write_bdr, "
+            "read_bdr) under a restated gradient driver" if kind == "reference" else
+            "the CPU restatement of the reference path (oracle/, FP32)")
+    sample = (f"{what}; each step: 1 shot, {r['nt']} of {shots[0].nt} time steps (forward, L2 misfit, rebuild, "
+              f"adjoint, imaging), {sample_s:.2f} s on {r['cores']} threads; ms_per_step = that time x {factor:.1f} "
+              f"(all {nshots} shots, every step)")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "steps": args.steps, "warmup": warm, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": describe(args, cfgkw, shots),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": "port", "sample": sample},
+            "extrapolated": {"sample_ms_per_step": sample_s * 1e3, "factor": factor,
+                             "timed_wall_s": sample_s * args.steps,
+                             "note": "each timed step runs a sample of the full gradient, so ms_per_step x steps "
+                                     "exceeds the run's wall time by the factor"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -249,7 +303,10 @@ def run_ours(args):
 
     cfgkw, vtrue, vstart, shots = workload(args, world, rank)
     nshots = len(shots)
-    cfg = fwigpu.make_config(**cfgkw, device=local, use_graph=0 if args.no_graph else 1)
+    store = {"auto": fwigpu.STORE_AUTO, "strips": fwigpu.STORE_STRIPS, "snapshots": fwigpu.STORE_SNAPSHOTS}[args.store]
+    cfg = fwigpu.make_config(**cfgkw, device=local, use_graph=0 if args.no_graph else 1, store=store,
+                             snapshots=args.snapshots, snap_precision=args.snap_precision,
+                             hbm_budget_mb=args.hbm_budget_mb)
     eng = fwigpu.Engine(cfg)
     stream = torch.cuda.Stream()
     eng.set_stream(stream.cuda_stream)
@@ -322,34 +379,45 @@ def run_ours(args):
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": describe(args, cfgkw, shots),
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": describe(args, cfgkw, shots, eng.stats()),
             "gcell_steps_per_s": gcell, "gpu_launches": launches, "clocks": clocks, "roofline": roof}
 
-    # end to end through the C ABI with pinned host buffers
+    # end to end through the C ABI with pinned host buffers: every step uploads the
+    # model and the observed traces and reads back the misfit and the (reduced) gradient
     if "e2e" not in skip:
         v_h = torch.empty(vstart.shape, dtype=torch.float32, pin_memory=True).numpy()
         v_h[:] = vstart
         o_h = torch.empty(obs.shape, dtype=torch.float32, pin_memory=True).numpy()
         o_h[:] = obs
-        g_h = torch.empty(vstart.shape, dtype=torch.float64, pin_memory=True).numpy()
+        g_pin = torch.empty(vstart.shape, dtype=torch.float64, pin_memory=True)
+        g_h = g_pin.numpy()
 
         def e2e_step():
             eng.set_model(v_h)
             eng.set_observed(o_h)
-            eng.gradient(out=g_h)
-            if dist:
-                gt = torch.from_numpy(g_h)
-                dist.all_reduce(gt.cuda())
-        e2e_step()
+            if not dist:
+                return eng.gradient(out=g_h)[0]
+            J, _ = eng.gradient(keep_on_device=True)
+            with torch.cuda.stream(stream):
+                mis_t.fill_(J)
+                shots_parallel.allreduce_gradient(grad_t, mis_t)
+                g_pin.view(-1).copy_(grad_t, non_blocking=True)
+            return mis_t
+        for _ in range(max(3, args.warmup)):
+            e2e_step()
         barrier()
-        k2 = max(1, min(args.steps, 3))
         e0.record(stream)
-        for _ in range(k2):
+        for _ in range(args.steps):
             e2e_step()
         e1.record(stream)
         barrier()
-        ms2 = e0.elapsed_time(e1) / k2
-        line["e2e"] = {"value": world * nshots / (ms2 / 1e3), "unit": UNIT, "ms_per_step": ms2,
+        ms2 = e0.elapsed_time(e1) / args.steps
+        if dist:
+            t = torch.tensor([ms2], device=f"cuda:{local}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms2 = float(t.item())
+        line["e2e"] = {"value": world * nshots / (ms2 / 1e3), "unit": UNIT, "ms_per_step": ms2, "steps": args.steps,
                        "h2d_bytes_per_step": int(v_h.nbytes + o_h.nbytes), "d2h_bytes_per_step": int(g_h.nbytes + 16)}
 
     # plain per-shot path (one shot per launch, shots one after another)
@@ -371,22 +439,38 @@ def run_ours(args):
         line["plain"] = {"shots": k, "value": k / (pms / 1e3), "unit": UNIT,
                          "batched_over_plain": value / world / (k / (pms / 1e3))}
 
-    # CPU baseline (the reference's path restated in oracle/) and the accuracy check
+    # checkpointed runs: the same gradient with the strip ring, at full size, on the GPU
+    if eng.stats()["store"] == fwigpu.STORE_SNAPSHOTS and "strips" not in skip and rank == 0:
+        import numpy as np
+        J_c, g_c = eng.gradient()
+        eng.close()
+        with fwigpu.Engine(fwigpu.make_config(**cfgkw, device=local, use_graph=1, store=fwigpu.STORE_STRIPS)) as se:
+            se.set_stream(stream.cuda_stream)
+            se.set_shots(shots)
+            se.set_model(vstart)
+            se.set_observed(obs)
+            J_s, g_s = se.gradient()
+        line["vs_strips"] = {"grad_rel_diff": float(np.linalg.norm(g_c - g_s) / np.linalg.norm(g_s)),
+                             "misfit_equal": bool(J_c == J_s),
+                             "note": "the strip ring's gradient is within 5e-6 of the FP64 oracle on C2"}
+
+    # CPU baseline (the reference's own kernels, or their restatement) and the accuracy check
     if "cpu" not in skip and rank == 0 and world == 1:
         def gpu_grad(nt, obs_sample):
-            import fwigpu as F
             s0 = shots[0]
-            sh = F.ShotSpec(s0.src_x, s0.src_z, s0.rec_xz, s0.wavelet[:nt])
-            c1 = F.make_config(**dict(cfgkw, nt_max=nt), device=local)
-            with F.Engine(c1) as e1_:
+            sh = fwigpu.ShotSpec(s0.src_x, s0.src_z, s0.rec_xz, s0.wavelet[:nt])
+            c1 = fwigpu.make_config(**dict(cfgkw, nt_max=nt), device=local)
+            with fwigpu.Engine(c1) as e1_:
                 e1_.set_shots([sh])
                 e1_.set_model(vstart)
                 e1_.set_observed(obs_sample)
                 return e1_.gradient()[1]
-        r = cpu_sample(args, cfgkw, vstart, vtrue, shots[:max(1, min(args.cpu_shots, nshots))], check_gpu=gpu_grad)
+        kind = cpu_kind()
+        r = cpu_sample(args, cfgkw, vstart, vtrue, shots[:max(1, min(args.cpu_shots, nshots))], args.cpu_steps,
+                       kind, check_gpu=gpu_grad)
         sec_shot = r["sec"] / r["shots"] * shots[0].nt / r["nt"]
-        line["cpu_baseline"] = {"value": 1.0 / sec_shot, "unit": UNIT, "cores": r["cores"], "kind": "port",
-                                "sample": f"{r['shots']} shots in one gradient, {r['nt']} of {shots[0].nt} steps, "
+        line["cpu_baseline"] = {"value": 1.0 / sec_shot, "unit": UNIT, "cores": r["cores"], "kind": kind,
+                                "sample": f"{r['shots']} shot(s) in one gradient, {r['nt']} of {shots[0].nt} steps, "
                                           f"FP32, {r['sec']:.2f} s" +
                                           ("" if r["nt"] == shots[0].nt else ", scaled linearly in steps")}
         line["accuracy"] = {"grad_rel_err_vs_fp64": r["grad_rel_err"],
@@ -394,7 +478,7 @@ def run_ours(args):
                             "sample": f"1 shot, {r['nt']} steps, workload grid"}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    eng.close()
+    eng.close()     # idempotent
     if dist:
         dist.destroy_process_group()
 

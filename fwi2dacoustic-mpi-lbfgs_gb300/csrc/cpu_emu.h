@@ -61,6 +61,27 @@ template <class T> inline T __ldg(const T* p) { return *p; }
 template <class T> inline T __ldcg(const T* p) { return *p; }
 template <class T> inline void __stcg(T* p, T v) { *p = v; }
 inline float atomicAdd(float* p, float v) { return std::atomic_ref<float>(*p).fetch_add(v); }
+inline unsigned atomicMax(unsigned* p, unsigned v)
+{
+    unsigned cur = std::atomic_ref<unsigned>(*p).load();
+    while (cur < v && !std::atomic_ref<unsigned>(*p).compare_exchange_weak(cur, v)) {}
+    return cur;
+}
+inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
+inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
+// 16-bit storage types of checkpoints: IEEE binary16 through the compiler's
+// _Float16 (round to nearest even), bfloat16 as the upper half of a float
+// rounded to nearest even by the usual bias of 0x7fff plus the kept LSB.
+struct __half { _Float16 v; };
+struct __nv_bfloat16 { unsigned short b; };
+inline __half __float2half_rn(float f) { return __half{(_Float16)f}; }
+inline float __half2float(__half h) { return (float)h.v; }
+inline __nv_bfloat16 __float2bfloat16_rn(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    return __nv_bfloat16{(unsigned short)((u + 0x7fffu + ((u >> 16) & 1u)) >> 16)};
+}
+inline float __bfloat162float(__nv_bfloat16 h) { return __uint_as_float((unsigned)h.b << 16); }
 inline int atomicCAS(int* p, int cmp, int val)
 {
     std::atomic_ref<int>(*p).compare_exchange_strong(cmp, val);
@@ -208,11 +229,14 @@ enum { cudaSuccess = 0, cudaErrorInvalidDevice = 101, cudaErrorNotSupported = 80
 enum cudaMemcpyKind { cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost, cudaMemcpyDeviceToDevice };
 enum { cudaStreamNonBlocking = 1, cudaEventDisableTiming = 2 };
 enum cudaStreamCaptureMode { cudaStreamCaptureModeThreadLocal };
+enum cudaStreamCaptureStatus { cudaStreamCaptureStatusNone, cudaStreamCaptureStatusActive };
 enum cudaFuncAttribute { cudaFuncAttributeMaxDynamicSharedMemorySize };
 struct cudaDeviceProp { int major = 10, minor = 3; };
 
 inline const char* cudaGetErrorString(cudaError_t e) { return e ? "emulation: not supported" : "no error"; }
 inline cudaError_t cudaGetLastError() { return cudaSuccess; }
+inline cudaError_t cudaPeekAtLastError() { return cudaSuccess; }
+inline cudaError_t cudaStreamIsCapturing(cudaStream_t, cudaStreamCaptureStatus* c) { *c = cudaStreamCaptureStatusNone; return cudaSuccess; }
 inline cudaError_t cudaGetDeviceCount(int* n) { *n = 1; return cudaSuccess; }
 inline cudaError_t cudaGetDeviceProperties(cudaDeviceProp* p, int) { *p = cudaDeviceProp{}; return cudaSuccess; }
 inline cudaError_t cudaSetDevice(int) { return cudaSuccess; }
@@ -226,6 +250,7 @@ template <class T> inline cudaError_t cudaMalloc(T** p, size_t n)
     return *p ? cudaSuccess : 2;
 }
 inline cudaError_t cudaFree(void* p) { std::free(p); return cudaSuccess; }
+inline cudaError_t cudaMemGetInfo(size_t* fr, size_t* tot) { *fr = *tot = (size_t)1 << 34; return cudaSuccess; }
 inline cudaError_t cudaMemcpy(void* d, const void* s, size_t n, cudaMemcpyKind) { std::memcpy(d, s, n); return cudaSuccess; }
 inline cudaError_t cudaMemcpyAsync(void* d, const void* s, size_t n, cudaMemcpyKind, cudaStream_t) { std::memcpy(d, s, n); return cudaSuccess; }
 inline cudaError_t cudaMemset(void* d, int v, size_t n) { std::memset(d, v, n); return cudaSuccess; }

@@ -141,6 +141,16 @@ struct fwi_ctx {
     std::vector<int> shot_tr0, shot_nr, shot_nt0; // first trace, traces, samples per trace
     int ntraces = 0;
     bool have_model = false, have_obs = false, have_fwd = false;
+    bool broken = false;           // a tile copy timed out: device state undefined, no further work
+    // forward-field storage (FWI_STORE_*): strips of every step, or checkpoints
+    // of the forward state at segment starts plus the strips of one segment
+    int store = FWI_STORE_STRIPS;
+    int seg = 0, nseg = 1;         // snapshots: segment length and count (strips: one segment)
+    int nsnap = 0;                 // checkpoints held: those of segments 1 .. nseg-2
+    void* snapP = nullptr;         // [nsnap][nshots][2][fstride] in snap_precision
+    float* snapPsi = nullptr;      // [nsnap][nshots][pl.stride]
+    unsigned* snapAmax = nullptr;  // [nsnap][nshots][2] absmax bits (F16 / BF16)
+    long long store_bytes = 0;
     size_t bytes_model = 0, bytes_shots = 0;
     std::string err;
     fwi_stats stats{};
@@ -193,8 +203,11 @@ void free_shots(fwi_ctx* x)
 {
     drop_graph(x);
     void* ps[] = {x->F, x->A, x->Gacc, x->psiF, x->psiA, x->ring, x->syn, x->res, x->obs, x->wav,
-                  x->shots_d, x->samp_d, x->recs_d, x->rtile_d, x->partial, x->mis, x->geo_d, x->xpart_d};
+                  x->shots_d, x->samp_d, x->recs_d, x->rtile_d, x->partial, x->mis, x->geo_d, x->xpart_d,
+                  x->snapP, x->snapPsi, x->snapAmax};
     for (void* p : ps) if (p) cudaFree(p);
+    x->snapP = nullptr; x->snapPsi = nullptr; x->snapAmax = nullptr;
+    x->store = FWI_STORE_STRIPS; x->seg = 0; x->nseg = 1; x->nsnap = 0; x->store_bytes = 0;
     x->F = x->A = x->Gacc = x->psiF = x->psiA = x->ring = x->syn = x->res = x->obs = x->wav = nullptr;
     x->shots_d = nullptr; x->samp_d = nullptr; x->recs_d = nullptr; x->rtile_d = nullptr;
     x->partial = nullptr; x->mis = nullptr; x->geo_d = nullptr; x->xpart_d = nullptr;
@@ -229,6 +242,8 @@ StepParams base_params(const fwi_ctx* x)
     P.res = x->res;
     P.ring = x->ring;
     P.strip_len = 2 * NSTRIP * (x->g.nx + x->g.nz);
+    P.ring_t0 = 0;
+    P.ring_slots = 0x7fffffff;
     P.jump = x->cfg.jump;
     return P;
 }
@@ -314,7 +329,7 @@ void join_classes(fwi_ctx* x)
 // One forward step of the shots [lo, hi): general tiles (one launch per
 // class, on the side streams) and interior tiles concurrently, then receiver
 // sampling.
-long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
+long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi, bool sample = true)
 {
     const dim3 block(BX, BY);
     const int n = hi - lo;
@@ -345,7 +360,7 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
         ++l;
     }
     join_classes(x);
-    if (P.step % x->cfg.jump == 0) {
+    if (sample && P.step % x->cfg.jump == 0) {
         RecParams Q = rec_params(x, P.pold, P.step);
         Q.lo = x->samp_off[lo];
         Q.hi = x->samp_off[hi];
@@ -402,6 +417,139 @@ long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
     return l;
 }
 
+// Field and psi buffers of forward step it (p^it in, p^{it+1} over p^{it-1}).
+void set_fwd_ptrs(const fwi_ctx* x, StepParams& P, int it)
+{
+    const long long half = (long long)x->nshots * x->g.fstride;
+    const long long phalf = (long long)x->nshots * x->pl.stride;
+    P.step = it;
+    P.pcur = x->F + (long long)(it & 1) * half + x->origin;
+    P.tm_pcur = x->tm_F[it & 1];
+    P.pold = x->F + (long long)((it + 1) & 1) * half + x->origin;
+    P.psr = x->psiF + (long long)(it & 1) * phalf;
+    P.psw = x->psiF + (long long)((it + 1) & 1) * phalf;
+}
+
+// Strip ring of segment j: with strips, every step's strip in its own slot;
+// with checkpoints, the strips of p^{t_a - 1} .. p^{t_a + seg} (t_a = j seg)
+// in seg + 2 slots.
+void set_ring(const fwi_ctx* x, StepParams& P, int j)
+{
+    if (x->store == FWI_STORE_STRIPS) {
+        P.ring_t0 = 0;
+        P.ring_slots = 0x7fffffff;
+    } else {
+        P.ring_t0 = j * x->seg - 2;
+        P.ring_slots = x->seg + 2;
+    }
+}
+
+// Grid of the checkpoint kernels: n shots, each thread both time levels of its cells.
+dim3 snap_grid(const fwi_ctx* x, int n)
+{
+    return dim3((unsigned)std::min<long long>(1024, (x->g.fstride + 255) / 256), 1, (unsigned)n);
+}
+
+// Checkpoint of segment j (its start t_a = j seg, taken after forward step
+// t_a - 1): p^{t_a} and p^{t_a - 1} (both field halves) and the psi memory
+// that step t_a reads, of shots [lo, hi).
+long long take_snapshot(fwi_ctx* x, int j, int lo, int hi)
+{
+    const int n = hi - lo;
+    if (n <= 0) return 0;
+    const Geo& g = x->g;
+    const long long half = (long long)x->nshots * g.fstride, phalf = (long long)x->nshots * x->pl.stride;
+    const long long blk = (long long)(j - 1) * x->nshots + lo;            // first (checkpoint, shot) block
+    const float* f = x->F + (long long)lo * g.fstride;
+    unsigned* amax = x->snapAmax + 2 * blk;
+    const dim3 grid = snap_grid(x, n);
+    const int ta = j * x->seg, ha = ta & 1;                                // p^{t_a} is in field half ha
+    long long l = 0;
+    switch (x->cfg.snap_precision) {
+    case FWI_SNAP_F32:
+        FWI_LAUNCH(k_snap_store<float>, grid, 256, 0, x->st, f, half, g.fstride, ha, nullptr,
+                   (float*)x->snapP + blk * 2 * g.fstride);
+        l = 1;
+        break;
+    case FWI_SNAP_F16:
+        cudaMemsetAsync(amax, 0, sizeof(unsigned) * 2 * n, x->st);
+        FWI_LAUNCH(k_snap_absmax, grid, 256, 0, x->st, f, half, g.fstride, ha, amax);
+        FWI_LAUNCH(k_snap_store<__half>, grid, 256, 0, x->st, f, half, g.fstride, ha, amax,
+                   (__half*)x->snapP + blk * 2 * g.fstride);
+        l = 2;
+        break;
+    default:
+        cudaMemsetAsync(amax, 0, sizeof(unsigned) * 2 * n, x->st);
+        FWI_LAUNCH(k_snap_absmax, grid, 256, 0, x->st, f, half, g.fstride, ha, amax);
+        FWI_LAUNCH(k_snap_store<__nv_bfloat16>, grid, 256, 0, x->st, f, half, g.fstride, ha, amax,
+                   (__nv_bfloat16*)x->snapP + blk * 2 * g.fstride);
+        l = 2;
+        break;
+    }
+    cudaMemcpyAsync(x->snapPsi + blk * x->pl.stride, x->psiF + (long long)(ta & 1) * phalf + (long long)lo * x->pl.stride,
+                    sizeof(float) * n * x->pl.stride, cudaMemcpyDeviceToDevice, x->st);
+    DIAG_SYNC("k_snap_store");
+    return l;
+}
+
+// Restores the checkpoint of segment j into the forward buffers of shots
+// [lo, hi) and writes the strips of the two time levels it holds, p^{t_a - 1}
+// and p^{t_a}, into ring slots 0 and 1 (P's ring is that of segment j).
+long long restore_snapshot(fwi_ctx* x, StepParams& P, int j, int lo, int hi)
+{
+    const int n = hi - lo;
+    if (n <= 0) return 0;
+    const Geo& g = x->g;
+    const long long half = (long long)x->nshots * g.fstride, phalf = (long long)x->nshots * x->pl.stride;
+    const long long blk = (long long)(j - 1) * x->nshots + lo;
+    float* f = x->F + (long long)lo * g.fstride;
+    const unsigned* amax = x->snapAmax + 2 * blk;
+    const dim3 grid = snap_grid(x, n);
+    const int ta = j * x->seg, ha = ta & 1;
+    switch (x->cfg.snap_precision) {
+    case FWI_SNAP_F32:
+        FWI_LAUNCH(k_snap_load<float>, grid, 256, 0, x->st, f, half, g.fstride, ha, nullptr,
+                   (const float*)x->snapP + blk * 2 * g.fstride);
+        break;
+    case FWI_SNAP_F16:
+        FWI_LAUNCH(k_snap_load<__half>, grid, 256, 0, x->st, f, half, g.fstride, ha, amax,
+                   (const __half*)x->snapP + blk * 2 * g.fstride);
+        break;
+    default:
+        FWI_LAUNCH(k_snap_load<__nv_bfloat16>, grid, 256, 0, x->st, f, half, g.fstride, ha, amax,
+                   (const __nv_bfloat16*)x->snapP + blk * 2 * g.fstride);
+        break;
+    }
+    cudaMemcpyAsync(x->psiF + (long long)(ta & 1) * phalf + (long long)lo * x->pl.stride, x->snapPsi + blk * x->pl.stride,
+                    sizeof(float) * n * x->pl.stride, cudaMemcpyDeviceToDevice, x->st);
+    const dim3 sgrid((P.strip_len + 255) / 256, 1, n);
+    P.shot_base = lo;
+    FWI_LAUNCH(k_strips_of_field, sgrid, 256, 0, x->st, P, x->F + (long long)((ta - 1) & 1) * half + x->origin, ta - 2);
+    FWI_LAUNCH(k_strips_of_field, sgrid, 256, 0, x->st, P, x->F + (long long)(ta & 1) * half + x->origin, ta - 1);
+    DIAG_SYNC("k_snap_load");
+    return 3;
+}
+
+// Forward steps [it0, it1) of the shots [lo, hi), each step over those of
+// them still active; receiver sampling and checkpoints only in the first
+// (full) forward pass.
+long long forward_steps(fwi_ctx* x, StepParams& P, int it0, int it1, int lo, int hi, bool first_pass)
+{
+    long long l = 0;
+    for (int it = it0; it < it1; ++it) {
+        const int h = std::min(hi, std::max(lo, active_slots(x, it + 1)));
+        if (h <= lo) break;
+        set_fwd_ptrs(x, P, it);
+        l += launch_fwd_step(x, P, lo, h, first_pass);
+        if (first_pass && x->store == FWI_STORE_SNAPSHOTS && (it + 1) % x->seg == 0) {
+            const int j = (it + 1) / x->seg;
+            if (j >= 1 && j <= x->nseg - 2)
+                l += take_snapshot(x, j, lo, std::min(hi, std::max(lo, active_slots(x, it + 2))));
+        }
+    }
+    return l;
+}
+
 int run_forward(fwi_ctx* x)
 {
     const long long half = (long long)x->nshots * x->g.fstride;
@@ -409,22 +557,13 @@ int run_forward(fwi_ctx* x)
     CK(cudaMemsetAsync(x->F, 0, sizeof(float) * 2 * half, x->st));
     CK(cudaMemsetAsync(x->psiF, 0, sizeof(float) * 2 * phalf, x->st));
     StepParams P = base_params(x);
+    set_ring(x, P, x->nseg - 1);             // the first pass keeps the strips of the last segment
     long long launches = 0;
     // batched: one launch per step over the active shots; plain: shot after shot
-    const int groups = x->cfg.plain_per_shot ? x->nshots : 1;
-    for (int grp = 0; grp < groups; ++grp) {
-        const int nt_grp = x->cfg.plain_per_shot ? x->nt_slot[grp] : x->nt_run;
-        for (int it = 0; it < nt_grp; ++it) {
-            const int lo = x->cfg.plain_per_shot ? grp : 0;
-            const int hi = x->cfg.plain_per_shot ? grp + 1 : active_slots(x, it + 1);
-            P.step = it;
-            P.pcur = x->F + (long long)(it & 1) * half + x->origin;
-            P.tm_pcur = x->tm_F[it & 1];
-            P.pold = x->F + (long long)((it + 1) & 1) * half + x->origin;
-            P.psr = x->psiF + (long long)(it & 1) * phalf;
-            P.psw = x->psiF + (long long)((it + 1) & 1) * phalf;
-            launches += launch_fwd_step(x, P, lo, hi);
-        }
+    if (x->cfg.plain_per_shot) {
+        for (int grp = 0; grp < x->nshots; ++grp) launches += forward_steps(x, P, 0, x->nt_slot[grp], grp, grp + 1, true);
+    } else {
+        launches += forward_steps(x, P, 0, x->nt_run, 0, x->nshots, true);
     }
     if (x->samp_used) {                                   // every sample lands before the misfit reads syn
         cudaEventRecord(x->samp_done, x->samp_st);
@@ -465,6 +604,65 @@ int run_misfit(fwi_ctx* x)
     return FWI_OK;
 }
 
+// Backward steps m = t_b .. t_a + 1 of shots [lo, hi) (each over those of them
+// still active).
+long long backward_steps(fwi_ctx* x, StepParams& P, int tb, int ta, int lo, int hi)
+{
+    const long long half = (long long)x->nshots * x->g.fstride;
+    const long long phalf = (long long)x->nshots * x->pl.stride;
+    long long l = 0;
+    for (int m = tb; m > ta; --m) {
+        const int h = std::min(hi, std::max(lo, active_slots(x, m)));
+        if (h <= lo) continue;
+        P.step = m;
+        P.pcur = x->F + (long long)((m - 1) & 1) * half + x->origin;   // p^{m-1}
+        P.tm_pcur = x->tm_F[(m - 1) & 1];
+        P.pold = x->F + (long long)(m & 1) * half + x->origin;         // p^m -> p^{m-2}
+        P.bcur = x->A + (long long)((m + 1) & 1) * half + x->origin;   // b^{m+1}
+        P.tm_bcur = x->tm_A[(m + 1) & 1];
+        P.bold = x->A + (long long)(m & 1) * half + x->origin;         // b^{m+2} -> b^m
+        P.psr = x->psiA + (long long)(m & 1) * phalf;
+        P.psw = x->psiA + (long long)((m + 1) & 1) * phalf;
+        l += launch_bwd_step(x, P, lo, h);
+    }
+    return l;
+}
+
+// The backward half of shots [lo, hi) whose longest record is nt_grp steps,
+// segment by segment, last first.  With strips there is one segment and the
+// forward pass left everything it needs.  With checkpoints, every segment
+// but the last (whose strips the forward pass kept) is first recomputed from
+// its checkpoint (segment 0 from rest), its strips going to the ring.
+long long backward_segments(fwi_ctx* x, StepParams& P, int nt_grp, int lo, int hi)
+{
+    const long long half = (long long)x->nshots * x->g.fstride;
+    const long long phalf = (long long)x->nshots * x->pl.stride;
+    const int seg = x->seg;
+    const int nseg_grp = (nt_grp + seg - 1) / seg;
+    long long l = 0;
+    for (int j = nseg_grp - 1; j >= 0; --j) {
+        const int ta = j * seg, tb = std::min(ta + seg, nt_grp);
+        set_ring(x, P, j);
+        if (x->store == FWI_STORE_SNAPSHOTS && j < x->nseg - 1) {
+            const int h = std::min(hi, std::max(lo, active_slots(x, ta + 1)));
+            if (h <= lo) continue;
+            if (j == 0) {
+                for (int k = 0; k < 2; ++k) {
+                    cudaMemsetAsync(x->F + k * half + (long long)lo * x->g.fstride, 0,
+                                    sizeof(float) * (h - lo) * x->g.fstride, x->st);
+                    cudaMemsetAsync(x->psiF + k * phalf + (long long)lo * x->pl.stride, 0,
+                                    sizeof(float) * (h - lo) * x->pl.stride, x->st);
+                }
+            } else {
+                l += restore_snapshot(x, P, j, lo, h);
+            }
+            l += forward_steps(x, P, ta, tb, lo, h, false);
+        }
+        l += backward_steps(x, P, tb, ta, lo, hi);
+    }
+    return l;
+}
+
 int run_backward(fwi_ctx* x)
 {
     const long long half = (long long)x->nshots * x->g.fstride;
@@ -475,23 +673,10 @@ int run_backward(fwi_ctx* x)
     StepParams P = base_params(x);
     P.gacc = x->Gacc + x->origin;
     long long launches = 0;
-    const int groups = x->cfg.plain_per_shot ? x->nshots : 1;
-    for (int grp = 0; grp < groups; ++grp) {
-        const int nt_grp = x->cfg.plain_per_shot ? x->nt_slot[grp] : x->nt_run;
-        for (int m = nt_grp; m >= 1; --m) {
-            const int lo = x->cfg.plain_per_shot ? grp : 0;
-            const int hi = x->cfg.plain_per_shot ? grp + 1 : active_slots(x, m);
-            P.step = m;
-            P.pcur = x->F + (long long)((m - 1) & 1) * half + x->origin;   // p^{m-1}
-            P.tm_pcur = x->tm_F[(m - 1) & 1];
-            P.pold = x->F + (long long)(m & 1) * half + x->origin;         // p^m -> p^{m-2}
-            P.bcur = x->A + (long long)((m + 1) & 1) * half + x->origin;   // b^{m+1}
-            P.tm_bcur = x->tm_A[(m + 1) & 1];
-            P.bold = x->A + (long long)(m & 1) * half + x->origin;         // b^{m+2} -> b^m
-            P.psr = x->psiA + (long long)(m & 1) * phalf;
-            P.psw = x->psiA + (long long)((m + 1) & 1) * phalf;
-            launches += launch_bwd_step(x, P, lo, hi);
-        }
+    if (x->cfg.plain_per_shot) {
+        for (int grp = 0; grp < x->nshots; ++grp) launches += backward_segments(x, P, x->nt_slot[grp], grp, grp + 1);
+    } else {
+        launches += backward_segments(x, P, x->nt_run, 0, x->nshots);
     }
     CK(cudaGetLastError());
     // FP64 reduction over shots and the 2/v factor
@@ -508,15 +693,27 @@ float event_ms(cudaEvent_t a, cudaEvent_t b)
     return ms;
 }
 
+// A block whose tile copy did not land within its bounded wait skipped its
+// tile and returned; the fields it should have written, and every later step,
+// are undefined.  The context then refuses further work (usable()).
 int finish(fwi_ctx* x)
 {
     CK(cudaStreamSynchronize(x->st));
     int bad = 0;
     CK(cudaMemcpy(&bad, x->err_d, sizeof(int), cudaMemcpyDeviceToHost));
     if (bad) {
-        cudaMemset(x->err_d, 0, sizeof(int));
-        return fail(x, FWI_ERR_CUDA, "a tile copy (TMA) did not complete within its bounded wait");
+        x->broken = true;
+        x->have_fwd = false;
+        return fail(x, FWI_ERR_CUDA, "a tile copy (TMA) did not complete within its bounded wait; the results are "
+                                     "undefined and the context refuses further work: destroy and recreate it");
     }
+    return FWI_OK;
+}
+
+int usable(fwi_ctx* x)
+{
+    if (x->broken)
+        return fail(x, FWI_ERR_STATE, "a tile copy timed out earlier: destroy and recreate the context");
     return FWI_OK;
 }
 
@@ -593,6 +790,67 @@ int run_phase(fwi_ctx* x, int ph, bool graph)
     return FWI_OK;
 }
 
+// Device bytes of the forward-field storage with nseg segments of
+// ceil(nt_run / nseg) steps: nseg - 2 checkpoints (two pressure fields in the
+// storage type, the psi memory and two scale words per shot) and a ring of
+// seg + 2 strip slots per shot.
+long long snapshot_bytes(const fwi_ctx* x, int nshots, int nt_run, int nseg)
+{
+    const long long seg = (nt_run + nseg - 1) / nseg;
+    const long long nseg_eff = (nt_run + seg - 1) / seg;
+    const long long elem = x->cfg.snap_precision == FWI_SNAP_F32 ? 4 : 2;
+    const long long per_ckpt = (long long)nshots * (2 * x->g.fstride * elem + 4 * x->pl.stride + 8);
+    const long long strip_b = 2LL * NSTRIP * (x->g.nx + x->g.nz) * 4;
+    return std::max(0LL, nseg_eff - 2) * per_ckpt + (seg + 2) * nshots * strip_b;
+}
+
+// Picks the forward-field storage of a shot set (cfg.store, FWI_STORE_AUTO:
+// the strip ring when the whole shot state fits the budget, else the segment
+// count with the least memory) and sets store, seg, nseg and nsnap.
+int choose_store(fwi_ctx* x, int nshots, int nt_run, long long base_b, long long strips_b)
+{
+    int mode = x->cfg.store;
+    int nseg = x->cfg.snapshots;
+    if (mode == FWI_STORE_AUTO) {
+        long long budget = (long long)x->cfg.hbm_budget_mb << 20;
+        if (!budget) {
+            size_t fr = 0, tot = 0;
+            if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); fr = 0; }
+            budget = (long long)(0.9 * (double)fr);
+        }
+        if (base_b + strips_b <= budget) {
+            mode = FWI_STORE_STRIPS;
+        } else {
+            long long best = -1;
+            for (int n = 1; n <= nt_run; ++n) {
+                const long long b = snapshot_bytes(x, nshots, nt_run, n);
+                if (best < 0 || b < best) { best = b; nseg = n; }
+                if (n > 4 && b > 2 * best) break;            // past the minimum: memory grows with n
+            }
+            if (base_b + best > budget)
+                return fail(x, FWI_ERR_NOMEM, "the shot state needs " + std::to_string((base_b + best) >> 20) +
+                                                  " MiB even with checkpoints; the budget is " +
+                                                  std::to_string(budget >> 20) + " MiB");
+            mode = FWI_STORE_SNAPSHOTS;
+        }
+    } else if (mode == FWI_STORE_SNAPSHOTS && nseg == 0) {
+        nseg = (int)std::ceil(std::sqrt((double)nt_run));
+    }
+    if (mode == FWI_STORE_STRIPS) {
+        x->store = FWI_STORE_STRIPS;
+        x->seg = nt_run;
+        x->nseg = 1;
+        x->nsnap = 0;
+        return FWI_OK;
+    }
+    nseg = std::max(1, std::min(nseg, nt_run));
+    x->store = FWI_STORE_SNAPSHOTS;
+    x->seg = (nt_run + nseg - 1) / nseg;
+    x->nseg = (nt_run + x->seg - 1) / x->seg;
+    x->nsnap = std::max(0, x->nseg - 2);
+    return FWI_OK;
+}
+
 // Traces longer than the XCORR kernel's shared memory holds?
 bool xcorr_too_long(const fwi_ctx* x)
 {
@@ -656,7 +914,10 @@ int fwi_check_config(const fwi_config* cfg)
     if (cfg->free_surface != 0 && cfg->free_surface != 1) return FWI_ERR_ARG;
     if ((cfg->use_graph != 0 && cfg->use_graph != 1) || (cfg->plain_per_shot != 0 && cfg->plain_per_shot != 1))
         return FWI_ERR_ARG;
-    for (int i = 0; i < 6; ++i) if (cfg->reserved[i]) return FWI_ERR_ARG;
+    if (cfg->store < FWI_STORE_AUTO || cfg->store > FWI_STORE_SNAPSHOTS || cfg->snapshots < 0 ||
+        cfg->snap_precision < FWI_SNAP_F32 || cfg->snap_precision > FWI_SNAP_BF16 || cfg->hbm_budget_mb < 0)
+        return FWI_ERR_ARG;
+    for (int i = 0; i < 2; ++i) if (cfg->reserved[i]) return FWI_ERR_ARG;
     return FWI_OK;
 }
 
@@ -923,6 +1184,15 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
 
     free_shots(x);
     const long long strip_len = 2LL * NSTRIP * (g.nx + g.nz);
+    {
+        const int nt_run = sd[order[0]].nt;
+        const long long half_b = (long long)nshots * g.fstride * 4, phalf_b = (long long)nshots * x->pl.stride * 4;
+        long long strips_b = 0;
+        for (int s = 0; s < nshots; ++s) strips_b += (long long)sd[s].nt * strip_len * 4;
+        const long long base_b = 5 * half_b + 4 * phalf_b + 4 * (3 * syn_off + wav_tot);
+        const int r = choose_store(x, nshots, nt_run, base_b, strips_b);
+        if (r) return r;
+    }
     std::vector<ShotDev> slot(nshots);
     std::vector<RecSample> samp;
     std::vector<RecDev> rec_all;
@@ -936,7 +1206,7 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
         const int s = order[k];
         ShotDev d = sd[s];
         d.ring_off = ring_off;
-        ring_off += (long long)d.nt * strip_len;
+        ring_off += (long long)(x->store == FWI_STORE_STRIPS ? d.nt : x->seg + 2) * strip_len;
         // sampling: one entry per receiver; injection: receivers grouped by
         // tile (CSR), summed inside the tile in receiver order
         std::vector<std::pair<int, RecDev>> tmp;
@@ -950,7 +1220,11 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
             rd.syn_base = recs[s][r].syn_base;
             tmp.push_back({(rz / TZ) * g.ntx + cx / TX, rd});
         }
-        std::stable_sort(tmp.begin(), tmp.end(), [](const auto& a, const auto& b2) { return a.first < b2.first; });
+        // by tile, then by cell; stable, so receivers that share a cell keep their
+        // input order and the backward sums them in that fixed order
+        std::stable_sort(tmp.begin(), tmp.end(), [](const auto& a, const auto& b2) {
+            return a.first != b2.first ? a.first < b2.first : a.second.cell < b2.second.cell;
+        });
         d.rtile_off = (int)rt_all.size();
         {
             std::vector<int> cnt(ntiles + 1, 0);
@@ -990,7 +1264,24 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     e = e ? e : dalloc(x, &x->mis, 2, &b);
     e = e ? e : dalloc(x, &x->geo_d, geo.size(), &b);
     e = e ? e : dalloc(x, &x->xpart_d, geo.size(), &b);
+    if (!e && x->nsnap > 0) {
+        const size_t nblk = (size_t)x->nsnap * nshots;
+        const size_t elem = x->cfg.snap_precision == FWI_SNAP_F32 ? 4 : 2;
+        unsigned char* sp = nullptr;
+        e = dalloc(x, &sp, nblk * 2 * g.fstride * elem, &b);
+        x->snapP = sp;
+        e = e ? e : dalloc(x, &x->snapPsi, nblk * x->pl.stride, &b);
+        e = e ? e : dalloc(x, &x->snapAmax, nblk * 2, &b);
+    }
     if (e) { std::string m = x->err; free_shots(x); x->err = m; return e; }
+    x->stats.store = x->store;
+    x->stats.segments = x->nseg;
+    x->stats.device_bytes = (long long)(x->bytes_model + x->bytes_shots);
+    x->store_bytes = (long long)ring_off * 4 +
+                     (x->nsnap > 0 ? (long long)x->nsnap * nshots *
+                                         (2 * g.fstride * (x->cfg.snap_precision == FWI_SNAP_F32 ? 4 : 2) +
+                                          4 * x->pl.stride + 8) : 0);
+    x->stats.store_bytes = x->store_bytes;
     for (int h = 0; h < 2; ++h)
         if (encode_field_map(&x->tm_F[h], x->F + h * half, g, x->rows_alloc, nshots) ||
             encode_field_map(&x->tm_A[h], x->A + h * half, g, x->rows_alloc, nshots)) {
@@ -1059,11 +1350,15 @@ static void record_stats(fwi_ctx* x, bool fwd, bool mis, bool bwd)
     x->stats.ms_total = event_ms(x->ev[6], x->ev[7]);
     x->stats.cell_steps = cs * ((fwd ? 1 : 0) + (bwd ? 2 : 0));
     x->stats.device_bytes = (long long)(x->bytes_model + x->bytes_shots);
+    x->stats.store = x->store;
+    x->stats.segments = x->nseg;
+    x->stats.store_bytes = x->store_bytes;
 }
 
 int fwi_forward(fwi_ctx* x, float* syn_out)
 {
     if (!x) return FWI_ERR_ARG;
+    if (usable(x)) return FWI_ERR_STATE;
     if (!x->have_model || !x->nshots) return fail(x, FWI_ERR_STATE, "fwi_set_model and fwi_set_shots first");
     CK(cudaSetDevice(x->cfg.device));
     CK(cudaEventRecord(x->ev[6], x->st));
@@ -1081,6 +1376,7 @@ int fwi_forward(fwi_ctx* x, float* syn_out)
 int fwi_backward(fwi_ctx* x, const float* residual, double* grad_out)
 {
     if (!x || !residual) return fail(x, FWI_ERR_ARG, "null argument");
+    if (usable(x)) return FWI_ERR_STATE;
     if (!x->have_fwd) return fail(x, FWI_ERR_STATE, "fwi_forward on the current model first");
     CK(cudaSetDevice(x->cfg.device));
     CK(cudaEventRecord(x->ev[6], x->st));
@@ -1101,6 +1397,7 @@ int fwi_backward(fwi_ctx* x, const float* residual, double* grad_out)
 static int gradient_impl(fwi_ctx* x, double* misfit)
 {
     if (!x) return FWI_ERR_ARG;
+    if (usable(x)) return FWI_ERR_STATE;
     if (!x->have_model || !x->nshots || !x->have_obs)
         return fail(x, FWI_ERR_STATE, "fwi_set_model, fwi_set_shots and fwi_set_observed first");
     CK(cudaSetDevice(x->cfg.device));
@@ -1152,16 +1449,23 @@ int fwi_gradient_f32(fwi_ctx* x, double* misfit, float* grad_out)
 
 const double* fwi_grad_device(const fwi_ctx* x) { return x ? x->grad : nullptr; }
 
-// Device address of g_noalloc_trace_sums for each device, looked up once per
-// device with that device current (host code cannot use the symbol itself).
-static double* noalloc_scratch(int device, cudaError_t* err)
+// Device address of g_noalloc_trace_sums on the current device.  The first
+// call on a device looks it up (cudaGetSymbolAddress, with that device
+// current) and keeps it.  Later calls look it up again whenever `st` is not
+// being captured, because a cudaDeviceReset reloads the module and may move
+// the array; during a capture they use the kept address, so the first call on
+// a device has to come before any capture.
+static double* noalloc_scratch(int device, cudaStream_t st, cudaError_t* err)
 {
     static std::mutex m;
     static double* addr[64] = {};
     *err = cudaSuccess;
     if (device < 0 || device >= 64) { *err = cudaErrorInvalidDevice; return nullptr; }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    *err = cudaStreamIsCapturing(st, &cap);
+    if (*err != cudaSuccess) return nullptr;
     std::lock_guard<std::mutex> lk(m);
-    if (!addr[device]) {
+    if (!addr[device] || cap == cudaStreamCaptureStatusNone) {
         double* p = nullptr;
         *err = cudaGetSymbolAddress((void**)&p, g_noalloc_trace_sums);
         if (*err != cudaSuccess) return nullptr;
@@ -1175,13 +1479,17 @@ int fwi_l2_misfit_noalloc(const float* syn, const float* obs, float* residual, i
 {
     if (!syn || !obs || !residual || !misfit || ntraces < 1 || nsamples < 1) return FWI_ERR_ARG;
     if (ntraces > FWI_NOALLOC_MAX_TRACES) return FWI_ERR_ARG;   // beyond the static scratch
+    // An error already pending on this thread belongs to the caller: leave it
+    // for them to read and launch nothing.
+    if (cudaPeekAtLastError() != cudaSuccess) return FWI_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return FWI_ERR_NODEVICE; }
-    cudaError_t e = cudaSuccess;
-    double* part = noalloc_scratch(dev, &e);
-    if (!part) { cudaGetLastError(); return FWI_ERR_CUDA; }
     cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    double* part = noalloc_scratch(dev, st, &e);
+    if (!part) { cudaGetLastError(); return FWI_ERR_CUDA; }
     FWI_LAUNCH(k_misfit_traces, ntraces, 256, 0, st, syn, obs, residual, nsamples, part);
+    if (cudaGetLastError() != cudaSuccess) return FWI_ERR_CUDA;     // this call's own launch error
     FWI_LAUNCH(k_misfit_final, 1, 256, 0, st, part, ntraces, misfit);
     if (cudaGetLastError() != cudaSuccess) return FWI_ERR_CUDA;
     return FWI_OK;

@@ -31,6 +31,8 @@
 #include "cpu_emu.h"
 #else
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
 #include "cpu_emu.h"
 #endif
 #include <stdint.h>
@@ -224,6 +226,8 @@ struct StepParams {
     const float* res;        // backward: adjoint sources
     float* ring;             // boundary strips
     int strip_len;
+    int ring_t0;             // the strip of p^{t+1} (saved at step t) sits in ring slot t - ring_t0
+    int ring_slots;          // slots per shot; strips whose slot falls outside are not saved
     int step;                // forward: it; backward: m
     int jump;
     int shot_base;           // slot of blockIdx.z == 0 (non-zero only when shots run one by one)
@@ -381,9 +385,11 @@ __device__ __forceinline__ void cp_async_wait()
 // Tensor-memory-access (TMA) copies of staged tiles: one thread arms an
 // mbarrier with the expected bytes and issues cp.async.bulk.tensor; every
 // thread waits on the barrier's phase 0.  The wait is bounded: a block whose
-// copy has not landed after TMA_WAIT_CYCLES (about half a second), or that
-// finds the flag already raised by another block, sets *err and skips its
-// tile, and the host reports the error.  Tile destinations are 128-byte
+// copy has not landed after its own TMA_WAIT_CYCLES (about half a second)
+// sets *err and skips its tile, and the host reports the error and refuses
+// further work on the context.  A block never gives up earlier (for example
+// because another block raised the flag), so it does not leave while its own
+// copy may still land in its shared memory.  Tile destinations are 128-byte
 // aligned; the x coordinate x0 - xoff is a multiple of 64 floats.
 constexpr long long TMA_WAIT_CYCLES = 1LL << 30;
 constexpr unsigned TILE_BYTES = SPH * SPW * sizeof(float);
@@ -420,7 +426,7 @@ __device__ __forceinline__ bool tma_wait(unsigned long long* bar, int* err)
     const long long t0 = clock64();
     for (unsigned i = 1;; ++i) {
         if (mbar_try_wait0(bar)) return true;
-        if ((i & 1023u) == 0 && (clock64() - t0 > TMA_WAIT_CYCLES || *(volatile int*)err)) break;
+        if ((i & 1023u) == 0 && clock64() - t0 > TMA_WAIT_CYCLES) break;
     }
     atomicExch(err, 1);
     return false;
@@ -446,7 +452,9 @@ __device__ __forceinline__ void save_strip(const StepParams& P, const ShotDev& s
     const Geo& g = P.g;
     const int iz = row - g.z0p, ix = c - g.x0p;
     if (iz < 0 || iz >= g.nz || ix < 0 || ix >= g.nx) return;
-    float* ring = P.ring + sd.ring_off + (long long)t * P.strip_len;
+    const int slot = t - P.ring_t0;
+    if ((unsigned)slot >= (unsigned)P.ring_slots) return;      // outside the ring of the current segment
+    float* ring = P.ring + sd.ring_off + (long long)slot * P.strip_len;
     if (iz < NSTRIP) *GP(ring + iz * g.nx + ix) = val;
     if (iz >= g.nz - NSTRIP) *GP(ring + (NSTRIP + g.nz - 1 - iz) * g.nx + ix) = val;
     float* lr = ring + 2 * NSTRIP * g.nx;
@@ -457,12 +465,33 @@ __device__ __forceinline__ void save_strip(const StepParams& P, const ShotDev& s
 __device__ __forceinline__ float load_strip(const StepParams& P, const ShotDev& sd, int iz, int ix, int t)
 {
     const Geo& g = P.g;
-    const float* ring = P.ring + sd.ring_off + (long long)t * P.strip_len;
+    const float* ring = P.ring + sd.ring_off + (long long)(t - P.ring_t0) * P.strip_len;
     if (iz < NSTRIP) return *GP(ring + iz * g.nx + ix);
     if (iz >= g.nz - NSTRIP) return *GP(ring + (NSTRIP + g.nz - 1 - iz) * g.nx + ix);
     const float* lr = ring + 2 * NSTRIP * g.nx;
     if (ix < NSTRIP) return *GP(lr + ix * g.nz + iz);
     return *GP(lr + (NSTRIP + g.nx - 1 - ix) * g.nz + iz);
+}
+
+// Adjoint sources of one tile: racc[cell] = the sum of res[r][k] over the
+// tile's receivers r in that cell.  The receivers of a tile, recs[rb, re),
+// are sorted by cell and, within a cell, by input order; the thread that
+// holds the first receiver of a cell adds up that run in order, so the sum
+// is the same on every run (no atomics).  racc must be zero beforehand.
+__device__ __forceinline__ void gather_residuals(const StepParams& P, int rb, int re, int k, float* racc)
+{
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    for (int q = rb + tid; q < re; q += NTH) {
+        const RecDev rd = *GP(P.recs + q);
+        if (q > rb && GP(P.recs + q - 1)->cell == rd.cell) continue;       // not the first of its cell
+        float sum = *GP(P.res + rd.syn_base + k);
+        for (int j = q + 1; j < re; ++j) {
+            const RecDev rn = *GP(P.recs + j);
+            if (rn.cell != rd.cell) break;
+            sum += *GP(P.res + rn.syn_base + k);
+        }
+        racc[SIDX(rd.cell, TZ * TX)] = sum;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1078,11 +1107,7 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
     if (do_res) {
         for (int q = tid; q < TZ * TX; q += NTH) sm.racc[SIDX(q, TZ * TX)] = 0.f;
         __syncthreads();
-        const int k = (m - 1) / P.jump;
-        for (int q = rb + tid; q < re; q += NTH) {
-            const RecDev rd = *GP(P.recs + q);
-            atomicAdd(&sm.racc[SIDX(rd.cell, TZ * TX)], *GP(P.res + rd.syn_base + k));
-        }
+        gather_residuals(P, rb, re, (m - 1) / P.jump, sm.racc);
     }
     cp_async_wait();
     __syncthreads();
@@ -1257,11 +1282,7 @@ __global__ void __launch_bounds__(NTH, 4) k_bwd_int(const __grid_constant__ Step
     if (do_res) {
         for (int q = tid; q < TZ * TX; q += NTH) sm.racc[SIDX(q, TZ * TX)] = 0.f;
         __syncthreads();
-        const int k = (m - 1) / P.jump;
-        for (int q = rb + tid; q < re; q += NTH) {
-            const RecDev rd = *GP(P.recs + q);
-            atomicAdd(&sm.racc[SIDX(rd.cell, TZ * TX)], *GP(P.res + rd.syn_base + k));
-        }
+        gather_residuals(P, rb, re, (m - 1) / P.jump, sm.racc);
     }
 #ifdef FWI_CPU_EMU
     __syncthreads();
@@ -1408,6 +1429,124 @@ __global__ void k_misfit_final(const double* __restrict__ partial, int n, double
         double v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
         v = warp_sum(v);
         if (threadIdx.x == 0) { out[0] = 0.5 * v; out[1] = 0.5 * v; }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoints of the forward state (FWI_STORE_SNAPSHOTS)
+// ---------------------------------------------------------------------------
+// The strips of field f (p^{t+1}, origin-based field layout) into ring
+// slot t - ring_t0, in save_strip's layout: [3 top rows | 3 bottom rows] x nx,
+// then [3 left columns | 3 right columns] x nz, for shots shot_base +
+// blockIdx.z.  Used after a checkpoint is restored, for the two time levels
+// it holds.
+__global__ void k_strips_of_field(const StepParams P, const float* __restrict__ f, int t)
+{
+    const Geo& g = P.g;
+    const int s = blockIdx.z + P.shot_base;
+    const ShotDev sd = *GP(P.shots + s);
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nud = 2 * NSTRIP * g.nx;
+    if (e >= P.strip_len) return;
+    int iz, ix;
+    if (e < nud) {
+        const int r = e / g.nx;
+        ix = e - r * g.nx;
+        iz = r < NSTRIP ? r : g.nz - 1 - (r - NSTRIP);
+    } else {
+        const int c = (e - nud) / g.nz;
+        iz = (e - nud) - c * g.nz;
+        ix = c < NSTRIP ? c : g.nx - 1 - (c - NSTRIP);
+    }
+    const float v = *GP(f + (long long)s * g.fstride + (long long)(iz + g.z0p) * g.ld + ix + g.x0p);
+    float* ring = P.ring + sd.ring_off + (long long)(t - P.ring_t0) * P.strip_len;
+    *GP(ring + e) = v;
+}
+
+// A checkpoint holds the two time levels of the forward field, p^{t_a} (in
+// field half ha) and p^{t_a - 1} (the other half), of gridDim.z shots of n
+// floats each (halves hs floats apart), laid out [shot][2][n].
+//   FP32: both levels, unscaled (exact copies).
+//   FP16 / BF16: level 0 = p^{t_a}, level 1 = d = p^{t_a} - p^{t_a - 1}, each
+//   scaled by its own absmax (stored = value * SNAP_RANGE / absmax).  Storing
+//   the difference keeps the error of the field's time derivative at the
+//   storage precision of d; two independently rounded levels would put an
+//   error of order (rounding of p) / (p^{t_a} - p^{t_a - 1}), tens of times
+//   larger, on it, and the recompute would propagate that as noise.
+// 2^14 keeps the largest value well inside FP16's range (65504) and the
+// smallest normal FP16 (6.1e-5) at 3.7e-9 of the absmax.
+constexpr float SNAP_RANGE = 16384.f;
+
+__device__ __forceinline__ float snap_scale_of(unsigned bits) { const float a = __uint_as_float(bits); return a > 0.f ? a / SNAP_RANGE : 1.f; }
+
+// Largest |p^{t_a}| and |p^{t_a} - p^{t_a-1}| of each shot, as the bits of
+// non-negative floats (which order like unsigned integers), in amax[2 s] and
+// amax[2 s + 1]; amax must be zero beforehand.
+__global__ void k_snap_absmax(const float* __restrict__ f, long long hs, long long n, int ha, unsigned* __restrict__ amax)
+{
+    const int s = blockIdx.z;
+    const float* pa = f + ha * hs + (long long)s * n;
+    const float* pb = f + (1 - ha) * hs + (long long)s * n;
+    float m0 = 0.f, m1 = 0.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float a = pa[i];
+        m0 = fmaxf(m0, fabsf(a));
+        m1 = fmaxf(m1, fabsf(a - pb[i]));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, o));
+        m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(amax + 2 * s, __float_as_uint(m0));
+        atomicMax(amax + 2 * s + 1, __float_as_uint(m1));
+    }
+}
+
+template <class T> __device__ __forceinline__ T snap_pack(float v);
+template <class T> __device__ __forceinline__ float snap_unpack(T q);
+template <> __device__ __forceinline__ float snap_pack<float>(float v) { return v; }
+template <> __device__ __forceinline__ float snap_unpack<float>(float q) { return q; }
+template <> __device__ __forceinline__ __half snap_pack<__half>(float v) { return __float2half_rn(v); }
+template <> __device__ __forceinline__ float snap_unpack<__half>(__half q) { return __half2float(q); }
+template <> __device__ __forceinline__ __nv_bfloat16 snap_pack<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+template <> __device__ __forceinline__ float snap_unpack<__nv_bfloat16>(__nv_bfloat16 q) { return __bfloat162float(q); }
+
+template <class T>
+__global__ void k_snap_store(const float* __restrict__ f, long long hs, long long n, int ha,
+                             const unsigned* __restrict__ amax, T* __restrict__ out)
+{
+    constexpr bool kDelta = sizeof(T) == 2;
+    const int s = blockIdx.z;
+    const float* pa = f + ha * hs + (long long)s * n;
+    const float* pb = f + (1 - ha) * hs + (long long)s * n;
+    T* q0 = out + 2LL * s * n;
+    T* q1 = q0 + n;
+    const float i0 = kDelta ? 1.f / snap_scale_of(amax[2 * s]) : 1.f;
+    const float i1 = kDelta ? 1.f / snap_scale_of(amax[2 * s + 1]) : 1.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float a = pa[i], b = pb[i];
+        q0[i] = snap_pack<T>(a * i0);
+        q1[i] = snap_pack<T>(kDelta ? (a - b) * i1 : b);
+    }
+}
+
+template <class T>
+__global__ void k_snap_load(float* __restrict__ f, long long hs, long long n, int ha,
+                            const unsigned* __restrict__ amax, const T* __restrict__ in)
+{
+    constexpr bool kDelta = sizeof(T) == 2;
+    const int s = blockIdx.z;
+    float* pa = f + ha * hs + (long long)s * n;
+    float* pb = f + (1 - ha) * hs + (long long)s * n;
+    const T* q0 = in + 2LL * s * n;
+    const T* q1 = q0 + n;
+    const float s0 = kDelta ? snap_scale_of(amax[2 * s]) : 1.f;
+    const float s1 = kDelta ? snap_scale_of(amax[2 * s + 1]) : 1.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float a = snap_unpack<T>(q0[i]) * s0;
+        pa[i] = a;
+        pb[i] = kDelta ? a - snap_unpack<T>(q1[i]) * s1 : snap_unpack<T>(q1[i]);
     }
 }
 

@@ -65,8 +65,51 @@ typedef struct fwi_config {
                               once and replay it as one CUDA graph */
     int   plain_per_shot;  /* 1: run shots one after another, one shot per
                               launch (the unbatched path, for comparison) */
-    int   reserved[6];     /* must be zero */
+    int   store;           /* how the backward half gets the forward field
+                              (FWI_STORE_*; 0 = FWI_STORE_AUTO) */
+    int   snapshots;       /* FWI_STORE_SNAPSHOTS: number of time segments,
+                              i.e. checkpoints of the forward state; 0 picks
+                              ceil(sqrt(nt)) */
+    int   snap_precision;  /* FWI_SNAP_F32 (0), FWI_SNAP_F16, FWI_SNAP_BF16:
+                              storage type of the checkpointed pressure fields */
+    int   hbm_budget_mb;   /* FWI_STORE_AUTO: device memory (MiB) the shot state
+                              may take; 0 = 90% of the free memory when
+                              fwi_set_shots runs */
+    int   reserved[2];     /* must be zero */
 } fwi_config;
+
+/* Forward-field storage for the backward half.
+ *
+ * FWI_STORE_STRIPS: the reference's boundary saving (write_bdr / read_bdr,
+ *   fwi_2d.c:882-960): the 2M-1 = 3 outer rows and columns of the physical
+ *   field of every step, an HBM ring of nt slots per shot in place of the
+ *   reference's nt_mem-chunked temp files (header.h:24).  The backward rebuilds
+ *   the source field in reverse time from them.
+ * FWI_STORE_SNAPSHOTS: checkpointing.  The time axis is cut into `snapshots`
+ *   segments of seg = ceil(nt/snapshots) steps; the forward pass keeps a
+ *   checkpoint of the forward state (p at two time levels and the CPML psi
+ *   memory) at every segment start and the strips of the last segment only.
+ *   The backward takes the segments last to first: it restores the segment's
+ *   checkpoint, recomputes the segment's forward steps into a strip ring of
+ *   seg + 2 slots, and rebuilds and images the segment from it.  Device
+ *   memory: (snapshots - 2) checkpoints plus seg + 2 strip slots per shot
+ *   instead of nt strip slots; cost: one more forward pass.  FWI_SNAP_F32
+ *   checkpoints are exact copies; the gradient then differs from
+ *   FWI_STORE_STRIPS by FP32 rounding only, because the reverse-time rebuild
+ *   restarts from recomputed fields at every segment instead of running
+ *   through the whole record.  With FWI_SNAP_F16 / FWI_SNAP_BF16 a
+ *   checkpoint holds p^{t_a} and the difference p^{t_a} - p^{t_a - 1}, each
+ *   scaled by its own per-checkpoint, per-shot absmax factor (the psi memory
+ *   stays FP32); the stencil arithmetic stays FP32.
+ * FWI_STORE_AUTO: the strip ring when the shot state fits hbm_budget_mb,
+ *   else snapshots with the segment count that needs the least memory (in
+ *   the storage type snap_precision); FWI_ERR_NOMEM when neither fits. */
+#define FWI_STORE_AUTO 0
+#define FWI_STORE_STRIPS 1
+#define FWI_STORE_SNAPSHOTS 2
+#define FWI_SNAP_F32 0
+#define FWI_SNAP_F16 1
+#define FWI_SNAP_BF16 2
 
 /* One shot.  Positions are metres, converted to cells as fwi_init does:
  * ix = round(x/dx), iz = round(z/dz - 0.5) (fwi_2d.c:363-371). */
@@ -86,6 +129,10 @@ typedef struct fwi_stats {
     double cell_steps;     /* physical cell-steps of the last gradient (x3 for fwd+rebuild+adjoint) */
     long long launches;    /* kernels launched by the last gradient */
     long long device_bytes;/* device memory held by the context */
+    int store;             /* storage in use: FWI_STORE_STRIPS or FWI_STORE_SNAPSHOTS */
+    int segments;          /* FWI_STORE_SNAPSHOTS: time segments (1 with strips) */
+    long long store_bytes; /* device memory of the forward-field storage
+                              (strip ring, or checkpoints plus segment ring) */
 } fwi_stats;
 
 typedef struct fwi_ctx fwi_ctx;
@@ -178,11 +225,16 @@ int fwi_version(void);
  * limit returns FWI_ERR_ARG.  Work is queued on `stream` (a cudaStream_t of
  * the current device, NULL for the default stream) and the call returns
  * without waiting.  The first call on each device looks up the scratch
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  Every call on a device uses the same scratch array, so calls
- * whose work overlaps on the GPU (different streams without ordering, or
- * other threads) race and must be serialised by the caller.  Each call
- * overwrites the scratch entries it reads, so nothing needs clearing. */
+ * address (cudaGetSymbolAddress, with that device current) and keeps it;
+ * make that first call before any stream capture.  Later calls look the
+ * address up again whenever `stream` is not being captured, so a
+ * cudaDeviceReset between calls is harmless.  If a CUDA error is already
+ * pending on the calling thread, the call returns FWI_ERR_CUDA without
+ * launching anything and leaves that error for the caller to read.  Every
+ * call on a device uses the same scratch array, so calls whose work overlaps
+ * on the GPU (different streams without ordering, or other threads) race
+ * and must be serialised by the caller.  Each call overwrites the scratch
+ * entries it reads, so nothing needs clearing. */
 #define FWI_NOALLOC_MAX_TRACES 65536
 int fwi_l2_misfit_noalloc(const float *syn, const float *obs, float *residual, int ntraces, int nsamples,
                           double *misfit, void *stream);

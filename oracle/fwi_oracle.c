@@ -132,6 +132,14 @@ void orc_model_ext(const float *model, int n1, int n2, float *emodel, int en1, i
 }
 
 /* FD coefficients, fwi_2d.c:304-314 (optimized 4th-order staggered pair). */
+/* Cell of a position in metres, fwi_2d.c:363-364: the float quotient, then
+ * C's round (half away from zero) in double, truncated to int. */
+void orc_cell_of(float x, float z, float dx, float dz, int *ix, int *iz)
+{
+    *ix = (int)round(x/dx);
+    *iz = (int)round(z/dz - 0.5);
+}
+
 void orc_fd_coeffs(float dx, float dz, float out[8])
 {
     coe_t c;

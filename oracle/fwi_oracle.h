@@ -71,6 +71,9 @@ void orc_model_ext(const float *model, int n1, int n2, float *emodel, int en1, i
  * out = {c0x, c1x, ix, c0z, c1z, iz, iz840, iz24}. */
 void orc_fd_coeffs(float dx, float dz, float out[8]);
 
+/* Cell (ix, iz) of a position (x, z) in metres, as fwi_2d.c:363-364. */
+void orc_cell_of(float x, float z, float dx, float dz, int *ix, int *iz);
+
 /* Padded-grid ekp = vext*vext*dt*dt (edge-replicated velocity). [pnz][pnx] */
 int  orc_ekp(const orc_config *cfg, const float *vel, float *ekp);
 

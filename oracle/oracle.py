@@ -7,8 +7,8 @@ Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
   restatement of the reference's propagator kernels (fwi_2d.c) and of the
   missing gradient driver ``grad4_1shot`` (header.h:283), FP32 and FP64 twins;
 * ``_ref/libfwiref.so`` (optional) -- the reference's own fwi_2d.c kernels
-  compiled from the reference checkout by ``make ref``; present only where the
-  reference sources are available.
+  compiled by ``make ref`` from the reference checkout or from its staged,
+  git-ignored copy in ``_ref/src``; present only where those sources are.
 """
 from __future__ import annotations
 
@@ -37,13 +37,24 @@ class OrcShot(C.Structure):
                 ("wav", C.POINTER(C.c_float))]
 
 
-def build(ref_dir: str | None = None, quiet: bool = True) -> None:
-    """Compile the oracle twins (and the reference kernels when available)."""
+STAGED = os.path.join(REFDIR, "src")
+
+
+def reference_sources() -> str | None:
+    """Directory with the reference's C sources and headers: the git-ignored
+    copy that ``make stage`` leaves in ``_ref/src`` (taken from the reference
+    checkout where it exists), or None where neither was ever present."""
+    return STAGED if os.path.isfile(os.path.join(STAGED, "fwi_2d.c")) else None
+
+
+def build(quiet: bool = True) -> None:
+    """Compile the oracle twins, and the reference's own kernels when their
+    sources are at hand (the checkout, or the staged copy of it)."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True, stdout=out)
-    ref_dir = ref_dir or "/root/reference"
-    if os.path.isfile(os.path.join(ref_dir, "fwi_2d.c")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_dir}"], check=True, stdout=out)
+    subprocess.run(["make", "-s", "-C", HERE, "stage"], check=True, stdout=out)
+    if reference_sources():
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, stdout=out)
 
 
 def _ptr(a, ctype):
@@ -92,6 +103,12 @@ class Oracle:
 
     def nt0(self, cfg):
         return (cfg.nt - 1) // cfg.jump + 1
+
+    def cell_of(self, x, z, dx, dz):
+        """Cell of a position in metres, fwi_2d.c:363-364."""
+        ix, iz = C.c_int(), C.c_int()
+        self.lib.orc_cell_of(C.c_float(x), C.c_float(z), C.c_float(dx), C.c_float(dz), C.byref(ix), C.byref(iz))
+        return ix.value, iz.value
 
     # -- single pieces ------------------------------------------------------------
     def cpml_coe(self, npml, d, dt, max_f=15.0, max_v=6000.0, coef_r=0.001):
@@ -281,6 +298,24 @@ class RefKernels:
         if st:
             raise ValueError(f"ref_forward failed: {st}")
         return syn, pf, pp, fs, rs
+
+    def gradient(self, cfg, vel, shots, obs_list, nt_mem=None):
+        """L2 gradient of the shots on the reference's own kernels
+        (ref_gradient in ref_driver.c: the timing path of the reference
+        arm).  nt_mem: steps per strip chunk written to the temp file; by
+        default the largest divisor of nt up to 200."""
+        if nt_mem is None:
+            nt_mem = max(d for d in range(1, min(cfg.nt, 200) + 1) if cfg.nt % d == 0)
+        vel = np.ascontiguousarray(vel, np.float32)
+        arr = (OrcShot * len(shots))(*[s.c for s in shots])
+        obs = np.ascontiguousarray(np.concatenate([np.asarray(o, np.float32).ravel() for o in obs_list]))
+        grad = np.zeros((cfg.nz, cfg.nx), np.float64)
+        mis = np.zeros(1, np.float64)
+        st = self.lib.ref_gradient(C.byref(cfg), _ptr(vel, C.c_float), len(shots), arr, _ptr(obs, C.c_float),
+                                   int(nt_mem), _ptr(mis, C.c_double), _ptr(grad, C.c_double))
+        if st:
+            raise ValueError(f"ref_gradient failed: {st}")
+        return float(mis[0]), grad
 
 
 # ---------------------------------------------------------------------------

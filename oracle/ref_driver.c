@@ -258,6 +258,117 @@ int ref_forward(const orc_config *cfg, const float *vel, const orc_shot *sh, int
     return 0;
 }
 
+/* Whole L2 gradient of nshots shots on the reference's own kernels (free
+ * surface), the CPU path the reference would run: per shot (one MPI rank
+ * each, MBotOpt.c:51,99, here one after another on all OpenMP threads)
+ *   forward   a_lap_opt_2d_pml + time_integral (fwi_2d.c:761-880), source
+ *             injection, receiver sampling, write_bdr chunked to a temp file
+ *             every nt_mem steps (fwi_2d.c:882-917);
+ *   misfit    J = 1/2 sum (syn - obs)^2, res = syn - obs;
+ *   backward  pml_var_init (fwi_2d.c:16-27), then per step the rebuild
+ *             a_lap_opt_2d + time_integral + read_bdr (fwi_2d.c:722-759,
+ *             866-880, 919-960) and the adjoint field with the reference's
+ *             forward operator a_lap_opt_2d_pml + time_integral (the
+ *             reference has no transposed operator), residuals injected at
+ *             the receivers, and the imaging g += b (ux + vz) of the rebuilt
+ *             field on the physical grid ((p^m - 2 p^{m-1} + p^{m-2}) / K on
+ *             the three outer rows and columns, which a_lap_opt_2d leaves);
+ *   gradient  (2 / v) sum over shots, FP64.
+ * It is the timing path of the reference arm: its gradient agrees with the
+ * exact-adjoint gradient of the oracle only approximately: the CPML
+ * operator is not self-adjoint. */
+int ref_gradient(const orc_config *cfg, const float *vel, int nshots, const orc_shot *shots,
+                 const float *obs, int nt_mem, double *misfit, double *grad)
+{
+    if (!cfg->free_surface || nt_mem < 1 || cfg->nt % nt_mem) return -1;
+    ref_plan *p = plan_new(cfg, nt_mem);
+    const fwi_shape *gf = &p->gf, *gb = &p->gb;
+    const int np = cfg->npml, nt = cfg->nt, jump = cfg->jump, nt0 = (nt-1)/jump + 1;
+    const int nx = cfg->nx, nz = cfg->nz;
+    const size_t npad = (size_t)gf->pnx*gf->pnz, nint = (size_t)gb->pnx*gb->pnz;
+    fwi_state fw, aw, bw;
+    state_alloc(&fw, gf); state_alloc(&aw, gf); state_alloc(&bw, gb);
+    float **vm = rows_of((float *)vel, nx, nz);
+    float **ekp = allocate2d(gf->pnx, gf->pnz);
+    model_ext(vm, nx, nz, ekp, gf->pnx, gf->pnz);
+    for (size_t i = 0; i < npad; i++) { float v = ekp[0][i]; ekp[0][i] = v*v*cfg->dt*cfg->dt; }
+    float **ekpi = (float **)malloc(sizeof(float *)*gb->pnz);
+    for (int i = 0; i < (int)gb->pnz; i++) ekpi[i] = ekp[i] + np;
+    const float iarea = 1.0/(cfg->dx*cfg->dz);   /* fwi_2d.c:216 */
+    float ***bc_ud = allocate3d(gb->pnx, 6, nt_mem), ***bc_lr = allocate3d(6, gb->pnz, nt_mem);
+    int offset = gb->pnx*6*nt_mem*sizeof(float) + gb->pnz*6*nt_mem*sizeof(float);   /* fwi_2d.c:391-392 */
+    double *gsum = (double *)calloc(nint, sizeof(double));
+    double J = 0;
+    size_t off = 0;
+    int st = 0;
+    for (int s = 0; s < nshots && !st; s++) {
+        const orc_shot *sh = &shots[s];
+        const int nr = sh->nr;
+        float *syn = (float *)calloc((size_t)nr*nt0 + 1, sizeof(float));
+        float *res = (float *)calloc((size_t)nr*nt0 + 1, sizeof(float));
+        FILE *fp = tmpfile();
+        if (!syn || !res || !fp) { st = -2; free(syn); free(res); if (fp) fclose(fp); break; }
+        state_var_init(&fw, (fwi_shape *)gf);
+        pml_var_init(&p->pml, (fwi_shape *)gf);
+        const int sx = sh->isx + np, sz = sh->isz;
+        for (int it = 0; it < nt; it++) {
+            a_lap_opt_2d_pml(fw.pnow, fw.u, fw.v, fw.ux, fw.vz, &p->coe, gf, &p->pml);
+            time_integral(fw.pnew, fw.pnow, fw.pold, fw.ux, fw.vz, ekp, gf->pnz, gf->pnx);
+            fw.pnew[sz][sx] += sh->wav[it]*iarea*ekp[sz][sx];
+            if (it % jump == 0)
+                for (int r = 0; r < nr; r++) syn[(size_t)r*nt0 + it/jump] = fw.pnew[sh->irz[r]][sh->irx[r]+np];
+            write_bdr(bc_ud, bc_lr, fw.pnew, gb, p->base, fp, it);
+            float **t = fw.pold; fw.pold = fw.pnow; fw.pnow = fw.pnew; fw.pnew = t;
+        }
+        for (size_t i = 0; i < (size_t)nr*nt0; i++) {
+            res[i] = syn[i] - obs[off + i];
+            J += 0.5*(double)res[i]*(double)res[i];
+        }
+        state_var_init(&aw, (fwi_shape *)gf);
+        state_var_init(&bw, (fwi_shape *)gb);
+        pml_var_init(&p->pml, (fwi_shape *)gf);
+        for (int iz = 0; iz < nz; iz++)
+            for (int ix = 0; ix < nx; ix++) {
+                bw.pold[iz][ix] = fw.pnow[iz][ix+np];   /* p^{nt}   */
+                bw.pnow[iz][ix] = fw.pold[iz][ix+np];   /* p^{nt-1} */
+            }
+        float **scratch = allocate2d(gb->pnx, gb->pnz);
+        read_bdr(bc_ud, bc_lr, scratch, gb, p->base, fp, offset, nt-1);
+        if (nt >= 2) read_bdr(bc_ud, bc_lr, scratch, gb, p->base, fp, offset, nt-2);
+        free2d(scratch);
+        for (int m = nt; m >= 1; m--) {
+            a_lap_opt_2d_pml(aw.pnow, aw.u, aw.v, aw.ux, aw.vz, &p->coe, gf, &p->pml);
+            time_integral(aw.pnew, aw.pnow, aw.pold, aw.ux, aw.vz, ekp, gf->pnz, gf->pnx);
+            if ((m-1) % jump == 0)
+                for (int r = 0; r < nr; r++)
+                    aw.pnew[sh->irz[r]][sh->irx[r]+np] += res[(size_t)r*nt0 + (m-1)/jump]*ekp[sh->irz[r]][sh->irx[r]+np];
+            a_lap_opt_2d(bw.pnow, bw.u, bw.v, bw.ux, bw.vz, &p->coe, gb);
+            time_integral(bw.pnew, bw.pnow, bw.pold, bw.ux, bw.vz, ekpi, gb->pnz, gb->pnx);
+            bw.pnew[sh->isz][sh->isx] += sh->wav[m-1]*iarea*ekpi[sh->isz][sh->isx];
+            if (m-3 >= 0) read_bdr(bc_ud, bc_lr, bw.pnew, gb, p->base, fp, offset, m-3);
+            #pragma omp parallel for
+            for (int iz = 0; iz < nz; iz++)
+                for (int ix = 0; ix < nx; ix++) {
+                    const int strip = iz < 3 || iz >= nz-3 || ix < 3 || ix >= nx-3;
+                    const float lp = strip ? ((bw.pold[iz][ix] - 2.0f*bw.pnow[iz][ix]) + bw.pnew[iz][ix])/ekpi[iz][ix]
+                                           : bw.ux[iz][ix] + bw.vz[iz][ix];
+                    gsum[(size_t)iz*nx + ix] += (double)(aw.pnew[iz][ix+np]*lp);
+                }
+            float **t = aw.pold; aw.pold = aw.pnow; aw.pnow = aw.pnew; aw.pnew = t;
+            t = bw.pold; bw.pold = bw.pnow; bw.pnow = bw.pnew; bw.pnew = t;
+        }
+        fclose(fp);
+        free(syn); free(res);
+        off += (size_t)nr*nt0;
+    }
+    for (size_t i = 0; i < nint; i++) grad[i] = gsum[i]*2.0/(double)vel[i];
+    if (misfit) misfit[0] = J;
+    free(gsum); free(ekpi);
+    free3d(bc_ud); free3d(bc_lr);
+    free2d(ekp); free(vm); state_free(&fw); state_free(&aw); state_free(&bw); plan_free(p);
+    return st;
+}
+
 /* ---- routines around the gradient ---------------------------------------
  * grad_precond_new5  grad_prec.c:5-52 (with triangle2, triangle_smooth.c:70-110,
  *                    and argmin/argmax, min_max.c)

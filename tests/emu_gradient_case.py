@@ -1,7 +1,11 @@
 """One gradient through the CPU emulation build of the engine, checked
 against the FP64 oracle; run by test_emu_sanitized.py in a child process
 with AddressSanitizer and UBSan preloaded and FWI_LIB pointing at
-libfwiemu.so.  Prints one JSON line {J, J64, grad_rel, syn_rel}."""
+libfwiemu.so.  Prints one JSON line {J, J64, grad_rel, syn_rel}.  With a
+fifth argument nseg > 0 the same gradient is also taken with checkpoints
+(FWI_STORE_SNAPSHOTS, nseg segments) in FP32 and FP16 storage (BF16 shares
+the FP16 path but for its rounding) and the line adds {snap_f32_rel,
+snap_f16_rel} (against FP64) and snap_f32_vs_strips."""
 import json
 import os
 import sys
@@ -17,7 +21,7 @@ import oracle as O                         # noqa: E402
 from test_gpu_parity import Case, rel      # noqa: E402
 
 
-def main(fs, nt, nx=150, nz=90):
+def main(fs, nt, nx=150, nz=90, nseg=0):
     o64 = O.Oracle("f64")
     case = Case(O, fs, seed=11 + fs, nt=nt, nx=nx, nz=nz)
     case.vtrue = (case.vel * 1.08).astype(np.float32)    # signal in the direct waves of a short record
@@ -34,7 +38,26 @@ def main(fs, nt, nx=150, nz=90):
         j, gg, _ = o64.gradient(case.oracle_cfg_for(len(s.wav)), case.vel, [s], [ob])
         J64 += j
         g64 += gg
-    print(json.dumps({"J": J, "J64": J64, "grad_rel": rel(g, g64), "syn_rel": syn_rel}))
+    out = {"J": J, "J64": J64, "grad_rel": rel(g, g64), "syn_rel": syn_rel}
+    if nseg:
+        import fwigpu
+        flat = np.concatenate([o.ravel() for o in obs])
+        for prec in ("f32", "f16"):
+            c = case.ecfg
+            cfg = fwigpu.make_config(c.nx, c.nz, c.dx, c.dz, c.dt, c.nt_max, npml=c.npml,
+                                     free_surface=c.free_surface, jump=c.jump, store=fwigpu.STORE_SNAPSHOTS,
+                                     snapshots=nseg, snap_precision=prec)
+            with fwigpu.Engine(cfg) as es:
+                es.set_shots(case.eshots)
+                es.set_model(case.vel)
+                es.set_observed(flat)
+                Js, gs = es.gradient()
+                st = es.stats()
+            assert st["store"] == fwigpu.STORE_SNAPSHOTS and st["segments"] == nseg, st
+            out[f"snap_{prec}_rel"] = rel(gs, g64)
+            if prec == "f32":
+                out["snap_f32_vs_strips"] = rel(gs, g)
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":

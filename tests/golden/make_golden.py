@@ -1,9 +1,11 @@
 """Generate the golden fixtures from the reference's OWN kernels.
 
-Run where the reference checkout is available (it is compiled by
-``make -C oracle ref REF=<checkout>`` into ``oracle/_ref/libfwiref.so``):
+Run where the reference's sources are at hand: the checkout named by
+``make -C oracle stage REF_CHECKOUT=<checkout>`` (which copies them, git-ignored,
+into ``oracle/_ref/src``) is compiled by ``make -C oracle ref`` into
+``oracle/_ref/libfwiref.so``:
 
-    python tests/golden/make_golden.py [<reference checkout>]
+    python tests/golden/make_golden.py [--aux]
 
 Writes ``tests/golden/ref_kernels.npz``: outputs of cpml_coe, model_ext,
 model_ext_fs_no, a_lap_opt_2d_pml (one step, with psi), a_lap_opt_2d,
@@ -122,8 +124,11 @@ def main_aux() -> None:
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
-def main(ref_dir: str) -> None:
-    O.build(ref_dir, quiet=False)
+def main() -> None:
+    O.build(quiet=False)
+    if not O.RefKernels.available():
+        raise SystemExit("the reference's kernels are not built: stage the reference sources first "
+                         "(make -C oracle stage REF_CHECKOUT=<checkout>)")
     if not O.RefKernels.available():
         raise SystemExit("reference kernels not built")
     ref = O.RefKernels()
@@ -153,7 +158,7 @@ def main(ref_dir: str) -> None:
 
 
 if __name__ == "__main__" and "--aux" in sys.argv:
-    O.build(next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference"), quiet=False)
+    O.build(quiet=False)
     main_aux()
 elif __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main()

@@ -61,6 +61,28 @@ def test_emulated_gradient_is_memory_safe_and_matches_oracle(emu_lib, oracles, f
     assert out["grad_rel"] <= GRAD_TOL, out
 
 
+def test_emulated_checkpointing_is_memory_safe(emu_lib, oracles):
+    """The checkpointed backward (5 segments of 9 steps over records of 41,
+    1 and 19 steps: restores, strip extraction, recompute, segments that
+    shots end in): memory safe; FP32 checkpoints within the gradient
+    tolerance of FP64 and within FP32 rounding of the strip ring's gradient
+    (the rebuild restarts from recomputed fields at every segment, so the
+    two differ in rounding only); FP16 checkpoints within 1e-3 of FP64 on
+    this short record (BF16 and the full-size errors are measured on the
+    GPU)."""
+    lib, libs = emu_lib
+    env = dict(os.environ, FWI_LIB=lib, LD_PRELOAD=" ".join(libs),
+               ASAN_OPTIONS="detect_leaks=0:abort_on_error=1", UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1")
+    r = subprocess.run([sys.executable, os.path.join(HERE, "emu_gradient_case.py"), "1", "41", "130", "70", "5"],
+                       capture_output=True, text=True, env=env, timeout=1200)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-6000:]
+    assert "ERROR: AddressSanitizer" not in r.stderr and "runtime error" not in r.stderr, r.stderr[-6000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["grad_rel"] <= GRAD_TOL, out
+    assert out["snap_f32_rel"] <= GRAD_TOL and out["snap_f32_vs_strips"] <= 1e-5, out
+    assert out["snap_f16_rel"] <= 1e-3, out
+
+
 def test_emulated_aux_routines_are_memory_safe_and_match_oracle(emu_lib, oracles):
     """fwi_grad_precond / fwi_bandpass bit-identical to the oracle, fwi_xcorr1d
     and the XCORR gradient within tolerance (tests/aux_cases.py)."""

@@ -52,8 +52,8 @@ class Case:
     @staticmethod
     def default_shots(rng, nx, nz, nt, jump, dt):
         shots = []
-        # surface shot, dense surface spread with a duplicated receiver cell
-        irx = np.concatenate([np.arange(0, nx, 2), [7, 7]])
+        # surface shot, dense surface spread with four receivers in one cell
+        irx = np.concatenate([np.arange(0, nx, 2), [7, 7, 7, 7]])
         shots.append((nx // 3, 1, irx, np.zeros_like(irx), ricker(nt, dt, 15.0)))
         # buried source inside the rebuilt interior, sparse receivers on all edges
         irx = np.array([0, nx - 1, 5, nx // 2, nx - 3, 2, 60])
