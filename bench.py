@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--snapshots", type=int, default=0, help="segments of the checkpointed backward (0: sqrt(nt))")
     ap.add_argument("--snap-precision", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--hbm-budget-mb", type=int, default=0, help="budget of --store auto (0: 90%% of free memory)")
+    ap.add_argument("--fd-order", type=int, default=4, choices=[4, 8], help="4: the reference's; 8: the extension")
     ap.add_argument("--skip", default="", help="comma list of: e2e,plain,cpu,strips")
     return ap.parse_args()
 
@@ -167,7 +168,7 @@ def describe(args, cfgkw, shots, stats=None):
             "nz": cfgkw["nz"], "nx": cfgkw["nx"], "npml": cfgkw["npml"], "shots": len(shots),
             "nt": nts[0] if len(nts) == 1 else [nts[0], nts[-1]],
             "receivers": nrs[0] if len(nrs) == 1 else [nrs[0], nrs[-1]],
-            "fd_order": 4, "free_surface": True, "checkpointing": ckpt,
+            "fd_order": args.fd_order, "free_surface": True, "checkpointing": ckpt,
             "store_gb": None if stats is None else stats["store_bytes"] / 1e9,
             "l2": "working set larger than L2 (no flush)", "parallelism": f"shots batched per launch",
             "data": "synthetic seeded model and acquisition; observed traces modelled on the true model"}
@@ -306,7 +307,7 @@ def run_ours(args):
     store = {"auto": fwigpu.STORE_AUTO, "strips": fwigpu.STORE_STRIPS, "snapshots": fwigpu.STORE_SNAPSHOTS}[args.store]
     cfg = fwigpu.make_config(**cfgkw, device=local, use_graph=0 if args.no_graph else 1, store=store,
                              snapshots=args.snapshots, snap_precision=args.snap_precision,
-                             hbm_budget_mb=args.hbm_budget_mb)
+                             hbm_budget_mb=args.hbm_budget_mb, fd_order=args.fd_order)
     eng = fwigpu.Engine(cfg)
     stream = torch.cuda.Stream()
     eng.set_stream(stream.cuda_stream)
@@ -444,7 +445,8 @@ def run_ours(args):
         import numpy as np
         J_c, g_c = eng.gradient()
         eng.close()
-        with fwigpu.Engine(fwigpu.make_config(**cfgkw, device=local, use_graph=1, store=fwigpu.STORE_STRIPS)) as se:
+        with fwigpu.Engine(fwigpu.make_config(**cfgkw, device=local, use_graph=1, store=fwigpu.STORE_STRIPS,
+                                              fd_order=args.fd_order)) as se:
             se.set_stream(stream.cuda_stream)
             se.set_shots(shots)
             se.set_model(vstart)

@@ -2,7 +2,8 @@
 
     python fwi2dacoustic-mpi-lbfgs_gb300/build.py [--force]
 
-Compiles ``csrc/fwi_engine.cu`` (which includes ``csrc/fwi_kernels.cuh``) and
+Compiles ``csrc/fwi_engine.cu`` (which includes ``csrc/fwi_kernels.cuh`` and
+``csrc/fwi_kernels8.cuh``) and
 ``csrc/fwi_aux.cu`` (``csrc/fwi_aux.cuh``) and ``csrc/fwi_lbfgs.cu`` with
 nvcc for ``-gencode arch=compute_103a,code=sm_103a`` into
 ``libfwigpu.so`` next to this file.  The CUDA runtime is linked statically so
@@ -19,7 +20,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 LIB = os.path.join(PKG, "libfwigpu.so")
 SOURCES = [os.path.join(PKG, "csrc", n) for n in ("fwi_engine.cu", "fwi_aux.cu", "fwi_lbfgs.cu")]
-DEPS = SOURCES + [os.path.join(PKG, "csrc", n) for n in ("fwi_kernels.cuh", "fwi_aux.cuh", "fwi_aux_kernels.cuh", "cpu_emu.h")] + \
+DEPS = SOURCES + [os.path.join(PKG, "csrc", n) for n in ("fwi_kernels.cuh", "fwi_kernels8.cuh", "fwi_aux.cuh",
+                                                       "fwi_aux_kernels.cuh", "cpu_emu.h")] + \
     [os.path.join(ROOT, "include", "fwi_gb300.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -7,6 +7,7 @@
 // every time step of every shot is one launch (grid.z = shot).
 #include "fwi_gb300.h"
 #include "fwi_kernels.cuh"
+#include "fwi_kernels8.cuh"
 #include "fwi_aux.cuh"
 #ifndef FWI_CPU_EMU
 #include <cudaTypedefs.h>
@@ -151,6 +152,13 @@ struct fwi_ctx {
     float* snapPsi = nullptr;      // [nsnap][nshots][pl.stride]
     unsigned* snapAmax = nullptr;  // [nsnap][nshots][2] absmax bits (F16 / BF16)
     long long store_bytes = 0;
+    // FD order: M = 2 (the reference's 4th order) or M = 4 (8th order, fwi_kernels8.cuh)
+    int M = 2, S = 3;              // half order, strip width 2M-1
+    float* X8 = nullptr;           // M = 4: u, v (or their adjoints), rebuild u, v: 4 x nshots x fstride
+    RecCell8* cells8_d = nullptr;  // M = 4: receiver cells of the backward injection, by slot
+    long long* rec8_d = nullptr;   // M = 4: syn offsets of the receivers, grouped by cell
+    int ncell8 = 0;
+    std::vector<int> cell8_off;    // M = 4: slot k's cells are cells8_d[cell8_off[k], cell8_off[k + 1])
     size_t bytes_model = 0, bytes_shots = 0;
     std::string err;
     fwi_stats stats{};
@@ -204,9 +212,10 @@ void free_shots(fwi_ctx* x)
     drop_graph(x);
     void* ps[] = {x->F, x->A, x->Gacc, x->psiF, x->psiA, x->ring, x->syn, x->res, x->obs, x->wav,
                   x->shots_d, x->samp_d, x->recs_d, x->rtile_d, x->partial, x->mis, x->geo_d, x->xpart_d,
-                  x->snapP, x->snapPsi, x->snapAmax};
+                  x->snapP, x->snapPsi, x->snapAmax, x->X8, x->cells8_d, x->rec8_d};
     for (void* p : ps) if (p) cudaFree(p);
     x->snapP = nullptr; x->snapPsi = nullptr; x->snapAmax = nullptr;
+    x->X8 = nullptr; x->cells8_d = nullptr; x->rec8_d = nullptr; x->ncell8 = 0;
     x->store = FWI_STORE_STRIPS; x->seg = 0; x->nseg = 1; x->nsnap = 0; x->store_bytes = 0;
     x->F = x->A = x->Gacc = x->psiF = x->psiA = x->ring = x->syn = x->res = x->obs = x->wav = nullptr;
     x->shots_d = nullptr; x->samp_d = nullptr; x->recs_d = nullptr; x->rtile_d = nullptr;
@@ -241,7 +250,7 @@ StepParams base_params(const fwi_ctx* x)
     P.syn = x->syn;
     P.res = x->res;
     P.ring = x->ring;
-    P.strip_len = 2 * NSTRIP * (x->g.nx + x->g.nz);
+    P.strip_len = 2 * x->S * (x->g.nx + x->g.nz);
     P.ring_t0 = 0;
     P.ring_slots = 0x7fffffff;
     P.jump = x->cfg.jump;
@@ -326,6 +335,49 @@ void join_classes(fwi_ctx* x)
         }
 }
 
+// 8th-order steps (fwi_kernels8.cuh): passes over the padded grid of the n
+// shots from P.shot_base, on the context's stream.
+Step8 step8_buffers(const fwi_ctx* x)
+{
+    const long long half = (long long)x->nshots * x->g.fstride;
+    return Step8{x->X8 + x->origin, x->X8 + half + x->origin, x->X8 + 2 * half + x->origin,
+                 x->X8 + 3 * half + x->origin};
+}
+
+long long launch_fwd_step8(fwi_ctx* x, StepParams& P, int n)
+{
+    const dim3 block(32, 8);
+    const dim3 gpos((x->g.pnx + 1 + 31) / 32, (x->g.pnz + 1 + 7) / 8, n), gcell((x->g.pnx + 31) / 32, (x->g.pnz + 7) / 8, n);
+    const Step8 B = step8_buffers(x);
+    FWI_LAUNCH(k8_uv, gpos, block, 0, x->st, P, B);
+    DIAG_SYNC("k8_uv");
+    FWI_LAUNCH(k8_fwd, gcell, block, 0, x->st, P, B);
+    DIAG_SYNC("k8_fwd");
+    return 2;
+}
+
+long long launch_bwd_step8(fwi_ctx* x, StepParams& P, int n)
+{
+    const dim3 block(32, 8);
+    const dim3 gpos((x->g.pnx + 1 + 31) / 32, (x->g.pnz + 1 + 7) / 8, n), gcell((x->g.pnx + 31) / 32, (x->g.pnz + 7) / 8, n);
+    const Step8 B = step8_buffers(x);
+    long long l = 3;
+    FWI_LAUNCH(k8_adj_uv, gpos, block, 0, x->st, P, B);
+    DIAG_SYNC("k8_adj_uv");
+    FWI_LAUNCH(k8_adj, gcell, block, 0, x->st, P, B);
+    DIAG_SYNC("k8_adj");
+    const int c0 = x->cell8_off[P.shot_base], nc = x->cell8_off[P.shot_base + n] - c0;
+    if ((P.step - 1) % x->cfg.jump == 0 && nc > 0) {
+        FWI_LAUNCH(k8_inject, (nc + 127) / 128, 128, 0, x->st, P, x->cells8_d + c0, x->rec8_d, nc,
+                   (P.step - 1) / x->cfg.jump);
+        DIAG_SYNC("k8_inject");
+        ++l;
+    }
+    FWI_LAUNCH(k8_rebuild, dim3((x->g.nx + 31) / 32, (x->g.nz + 7) / 8, n), block, 0, x->st, P, B);
+    DIAG_SYNC("k8_rebuild");
+    return l;
+}
+
 // One forward step of the shots [lo, hi): general tiles (one launch per
 // class, on the side streams) and interior tiles concurrently, then receiver
 // sampling.
@@ -339,6 +391,9 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi, bool sample
         cudaStreamWaitEvent(x->st, x->samp_ev[P.step & 1], 0);
         x->samp_pending[P.step & 1] = false;
     }
+    if (x->M == 4) {
+        l += launch_fwd_step8(x, P, n);
+    } else {
     fork_classes(x);
     const int2* gen = P.gen_tiles;
     for (const int cls : kClassOrder) {
@@ -360,6 +415,7 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi, bool sample
         ++l;
     }
     join_classes(x);
+    }
     if (sample && P.step % x->cfg.jump == 0) {
         RecParams Q = rec_params(x, P.pold, P.step);
         Q.lo = x->samp_off[lo];
@@ -392,6 +448,7 @@ long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
     const int n = hi - lo;
     long long l = 0;
     P.shot_base = lo;
+    if (x->M == 4) return launch_bwd_step8(x, P, n);
     fork_classes(x);
     // z-only tiles never touch srx (the last member of BwdSmem)
     const int2* gen = P.gen_tiles;
@@ -524,8 +581,11 @@ long long restore_snapshot(fwi_ctx* x, StepParams& P, int j, int lo, int hi)
                     sizeof(float) * n * x->pl.stride, cudaMemcpyDeviceToDevice, x->st);
     const dim3 sgrid((P.strip_len + 255) / 256, 1, n);
     P.shot_base = lo;
-    FWI_LAUNCH(k_strips_of_field, sgrid, 256, 0, x->st, P, x->F + (long long)((ta - 1) & 1) * half + x->origin, ta - 2);
-    FWI_LAUNCH(k_strips_of_field, sgrid, 256, 0, x->st, P, x->F + (long long)(ta & 1) * half + x->origin, ta - 1);
+    for (int lev = 0; lev < 2; ++lev) {                    // p^{t_a - 1}, then p^{t_a}
+        const float* f = x->F + (long long)((ta - 1 + lev) & 1) * half + x->origin;
+        if (x->S == NSTRIP8) FWI_LAUNCH(k_strips_of_field<NSTRIP8>, sgrid, 256, 0, x->st, P, f, ta - 2 + lev);
+        else FWI_LAUNCH(k_strips_of_field<NSTRIP>, sgrid, 256, 0, x->st, P, f, ta - 2 + lev);
+    }
     DIAG_SYNC("k_snap_load");
     return 3;
 }
@@ -800,7 +860,7 @@ long long snapshot_bytes(const fwi_ctx* x, int nshots, int nt_run, int nseg)
     const long long nseg_eff = (nt_run + seg - 1) / seg;
     const long long elem = x->cfg.snap_precision == FWI_SNAP_F32 ? 4 : 2;
     const long long per_ckpt = (long long)nshots * (2 * x->g.fstride * elem + 4 * x->pl.stride + 8);
-    const long long strip_b = 2LL * NSTRIP * (x->g.nx + x->g.nz) * 4;
+    const long long strip_b = 2LL * x->S * (x->g.nx + x->g.nz) * 4;
     return std::max(0LL, nseg_eff - 2) * per_ckpt + (seg + 2) * nshots * strip_b;
 }
 
@@ -917,7 +977,8 @@ int fwi_check_config(const fwi_config* cfg)
     if (cfg->store < FWI_STORE_AUTO || cfg->store > FWI_STORE_SNAPSHOTS || cfg->snapshots < 0 ||
         cfg->snap_precision < FWI_SNAP_F32 || cfg->snap_precision > FWI_SNAP_BF16 || cfg->hbm_budget_mb < 0)
         return FWI_ERR_ARG;
-    for (int i = 0; i < 2; ++i) if (cfg->reserved[i]) return FWI_ERR_ARG;
+    if (cfg->fd_order != 0 && cfg->fd_order != 4 && cfg->fd_order != 8) return FWI_ERR_ARG;
+    if (cfg->reserved[0]) return FWI_ERR_ARG;
     return FWI_OK;
 }
 
@@ -1030,6 +1091,15 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     c.c0x = fd[0]; c.c1x = fd[1]; c.ix = fd[2]; c.c0z = fd[3]; c.c1z = fd[4]; c.iz = fd[5];
     c.iz840 = fd[6]; c.iz24 = fd[7];
     c.iarea = 1.0 / (cfg->dx * cfg->dz);                    // fwi_2d.c:216
+    x->M = cfg->fd_order == 8 ? 4 : 2;
+    x->S = 2 * x->M - 1;
+    {   // 8th-order staggered weights / h, w_k / h rounded to float
+        static const double w[4] = {1225.0 / 1024.0, -245.0 / 3072.0, 49.0 / 5120.0, -5.0 / 7168.0};
+        for (int k = 0; k < 4; ++k) {
+            c.w8x[k] = (float)(w[k] / (double)cfg->dx);
+            c.w8z[k] = (float)(w[k] / (double)cfg->dz);
+        }
+    }
     {   // D- D+ along x in one symmetric 7-point stencil (interior tiles)
         const double a = c.c0x, b = c.c1x;
         c.wx1 = (float)(a * a - 2.0 * a * b);
@@ -1112,8 +1182,11 @@ int fwi_set_model(fwi_ctx* x, const float* vel)
         if (!(v > 0.f)) return fail(x, FWI_ERR_ARG, "non-positive velocity at index " + std::to_string(i));
         vmax = std::max(vmax, v);
     }
-    // leapfrog stability of the 4th-order staggered pair: v dt (|c0|+|c1|) sqrt(1/dx^2+1/dz^2) <= 1
-    const double cfl = (double)vmax * x->cfg.dt * (1.129042 + 0.04301412) *
+    // leapfrog stability of the staggered pair: v dt sum|w_k| sqrt(1/dx^2+1/dz^2) <= 1, with the
+    // 4th-order pair (fwi_2d.c:307-311) or the 8th-order weights
+    const double wsum = x->M == 4 ? 1225.0 / 1024.0 + 245.0 / 3072.0 + 49.0 / 5120.0 + 5.0 / 7168.0
+                                  : 1.129042 + 0.04301412;
+    const double cfl = (double)vmax * x->cfg.dt * wsum *
                        std::sqrt(1.0 / ((double)x->cfg.dx * x->cfg.dx) + 1.0 / ((double)x->cfg.dz * x->cfg.dz));
     if (cfl > 1.0) return fail(x, FWI_ERR_CFL, "CFL number " + std::to_string(cfl) + " > 1");
     CK(cudaSetDevice(x->cfg.device));
@@ -1183,7 +1256,7 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sd[a].nt > sd[b].nt; });
 
     free_shots(x);
-    const long long strip_len = 2LL * NSTRIP * (g.nx + g.nz);
+    const long long strip_len = 2LL * x->S * (g.nx + g.nz);
     {
         const int nt_run = sd[order[0]].nt;
         const long long half_b = (long long)nshots * g.fstride * 4, phalf_b = (long long)nshots * x->pl.stride * 4;
@@ -1198,6 +1271,9 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     std::vector<RecDev> rec_all;
     std::vector<int> rt_all;
     std::vector<float> wav_all(wav_tot);
+    std::vector<RecCell8> cells8;
+    std::vector<long long> rec8;
+    x->cell8_off.assign(nshots + 1, 0);
     long long ring_off = 0;
     const int ntiles = g.ntx * g.ntz;
     x->nt_slot.resize(nshots);
@@ -1235,6 +1311,19 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
             for (auto& t : tmp) rec_all.push_back(t.second);
         }
         x->samp_off[k + 1] = (int)samp.size();
+        if (x->M == 4) {           // receiver cells of the 8th-order injection: by cell, input order inside
+            std::vector<int> ord(recs[s].size());
+            for (size_t r = 0; r < ord.size(); ++r) ord[r] = (int)r;
+            std::stable_sort(ord.begin(), ord.end(), [&](int a, int b2) { return recs[s][a].foff < recs[s][b2].foff; });
+            for (size_t q = 0; q < ord.size(); ++q) {
+                const Rec& rr = recs[s][ord[q]];
+                if (q == 0 || rr.foff != recs[s][ord[q - 1]].foff)
+                    cells8.push_back(RecCell8{k, (int)rec8.size(), 0, 0, rr.foff});
+                ++cells8.back().count;
+                rec8.push_back(rr.syn_base);
+            }
+            x->cell8_off[k + 1] = (int)cells8.size();
+        }
         std::memcpy(&wav_all[wav_off[s]], shots[s].wavelet, sizeof(float) * shots[s].nt);
         slot[k] = d;
         x->nt_slot[k] = d.nt;
@@ -1264,6 +1353,12 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
     e = e ? e : dalloc(x, &x->mis, 2, &b);
     e = e ? e : dalloc(x, &x->geo_d, geo.size(), &b);
     e = e ? e : dalloc(x, &x->xpart_d, geo.size(), &b);
+    if (!e && x->M == 4) {
+        e = dalloc(x, &x->X8, 4 * half, &b);
+        e = e ? e : dalloc(x, &x->cells8_d, cells8.size(), &b);
+        e = e ? e : dalloc(x, &x->rec8_d, rec8.size(), &b);
+        x->ncell8 = (int)cells8.size();
+    }
     if (!e && x->nsnap > 0) {
         const size_t nblk = (size_t)x->nsnap * nshots;
         const size_t elem = x->cfg.snap_precision == FWI_SNAP_F32 ? 4 : 2;
@@ -1294,6 +1389,14 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
         CK(cudaMemcpyAsync(x->recs_d, rec_all.data(), sizeof(RecDev) * rec_all.size(), cudaMemcpyHostToDevice, x->st));
     }
     CK(cudaMemcpyAsync(x->rtile_d, rt_all.data(), sizeof(int) * rt_all.size(), cudaMemcpyHostToDevice, x->st));
+    if (x->M == 4) {
+        // zero buffers: positions a pass never writes (outside its range) read as 0
+        CK(cudaMemsetAsync(x->X8, 0, sizeof(float) * 4 * half, x->st));
+        if (!cells8.empty()) {
+            CK(cudaMemcpyAsync(x->cells8_d, cells8.data(), sizeof(RecCell8) * cells8.size(), cudaMemcpyHostToDevice, x->st));
+            CK(cudaMemcpyAsync(x->rec8_d, rec8.data(), sizeof(long long) * rec8.size(), cudaMemcpyHostToDevice, x->st));
+        }
+    }
     CK(cudaMemcpyAsync(x->wav, wav_all.data(), sizeof(float) * wav_all.size(), cudaMemcpyHostToDevice, x->st));
     if (!geo.empty()) CK(cudaMemcpyAsync(x->geo_d, geo.data(), sizeof(float4) * geo.size(), cudaMemcpyHostToDevice, x->st));
     x->shot_syn_off = tr_syn_off;

@@ -130,6 +130,7 @@ struct Coef {
     float c0x, c1x, ix, c0z, c1z, iz, iz840, iz24;   // fwi_2d.c:304-314
     float iarea;                                     // fwi_2d.c:216
     float wx1, wx2, wx3;                             // dxx7 weights (from c0x, c1x)
+    float w8x[4], w8z[4];                            // 8th-order staggered weights / h (fd_order 8)
 };
 
 // The x part of the plain operator, ux(c) = c0 (u(c+1) - u(c)) + c1 (u(c+2) -
@@ -1435,28 +1436,29 @@ __global__ void k_misfit_final(const double* __restrict__ partial, int n, double
 // ---------------------------------------------------------------------------
 // Checkpoints of the forward state (FWI_STORE_SNAPSHOTS)
 // ---------------------------------------------------------------------------
-// The strips of field f (p^{t+1}, origin-based field layout) into ring
-// slot t - ring_t0, in save_strip's layout: [3 top rows | 3 bottom rows] x nx,
-// then [3 left columns | 3 right columns] x nz, for shots shot_base +
-// blockIdx.z.  Used after a checkpoint is restored, for the two time levels
+// The strips (NS = 2M-1 wide) of field f (p^{t+1}, origin-based field
+// layout) into ring slot t - ring_t0, in save_strip's layout: [NS top rows |
+// NS bottom rows] x nx, then [NS left columns | NS right columns] x nz, for
+// shots shot_base + blockIdx.z.  Used after a checkpoint is restored, for the two time levels
 // it holds.
+template <int NS>
 __global__ void k_strips_of_field(const StepParams P, const float* __restrict__ f, int t)
 {
     const Geo& g = P.g;
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nud = 2 * NSTRIP * g.nx;
+    const int nud = 2 * NS * g.nx;
     if (e >= P.strip_len) return;
     int iz, ix;
     if (e < nud) {
         const int r = e / g.nx;
         ix = e - r * g.nx;
-        iz = r < NSTRIP ? r : g.nz - 1 - (r - NSTRIP);
+        iz = r < NS ? r : g.nz - 1 - (r - NS);
     } else {
         const int c = (e - nud) / g.nz;
         iz = (e - nud) - c * g.nz;
-        ix = c < NSTRIP ? c : g.nx - 1 - (c - NSTRIP);
+        ix = c < NS ? c : g.nx - 1 - (c - NS);
     }
     const float v = *GP(f + (long long)s * g.fstride + (long long)(iz + g.z0p) * g.ld + ix + g.x0p);
     float* ring = P.ring + sd.ring_off + (long long)(t - P.ring_t0) * P.strip_len;

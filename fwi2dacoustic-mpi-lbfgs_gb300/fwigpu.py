@@ -33,7 +33,7 @@ class FwiConfig(C.Structure):
                 ("pml_max_f", C.c_float), ("pml_max_v", C.c_float), ("pml_coef_r", C.c_float),
                 ("device", C.c_int), ("use_graph", C.c_int), ("plain_per_shot", C.c_int),
                 ("store", C.c_int), ("snapshots", C.c_int), ("snap_precision", C.c_int),
-                ("hbm_budget_mb", C.c_int), ("reserved", C.c_int * 2)]
+                ("hbm_budget_mb", C.c_int), ("fd_order", C.c_int), ("reserved", C.c_int * 1)]
 
 
 class FwiShot(C.Structure):
@@ -137,11 +137,13 @@ SNAP_PRECISION = {"f32": SNAP_F32, "f16": SNAP_F16, "bf16": SNAP_BF16}
 
 def make_config(nx, nz, dx, dz, dt, nt_max, npml=20, free_surface=1, jump=1, pml_max_f=15.0,
                 pml_max_v=6000.0, pml_coef_r=0.001, device=0, use_graph=0, plain_per_shot=0,
-                store=STORE_AUTO, snapshots=0, snap_precision=SNAP_F32, hbm_budget_mb=0) -> FwiConfig:
+                store=STORE_AUTO, snapshots=0, snap_precision=SNAP_F32, hbm_budget_mb=0,
+                fd_order=4) -> FwiConfig:
     """CPML defaults are MAX_F, MAX_V, COEF_R of fwi_sys.h:2-4.  ``store``:
     STORE_AUTO / STORE_STRIPS / STORE_SNAPSHOTS; ``snapshots``: segments of
     the checkpointed backward (0 = ceil(sqrt(nt))); ``snap_precision``:
-    SNAP_F32 / SNAP_F16 / SNAP_BF16 (or "f32", "f16", "bf16")."""
+    SNAP_F32 / SNAP_F16 / SNAP_BF16 (or "f32", "f16", "bf16"); ``fd_order``:
+    4 (the reference's) or 8."""
     cfg = FwiConfig()
     cfg.nx, cfg.nz, cfg.dx, cfg.dz, cfg.dt = nx, nz, dx, dz, dt
     cfg.nt_max, cfg.npml, cfg.free_surface, cfg.jump = nt_max, npml, int(free_surface), jump
@@ -149,6 +151,7 @@ def make_config(nx, nz, dx, dz, dt, nt_max, npml=20, free_surface=1, jump=1, pml
     cfg.device, cfg.use_graph, cfg.plain_per_shot = device, use_graph, plain_per_shot
     cfg.store, cfg.snapshots, cfg.hbm_budget_mb = store, snapshots, hbm_budget_mb
     cfg.snap_precision = SNAP_PRECISION.get(snap_precision, snap_precision)
+    cfg.fd_order = fd_order
     return cfg
 
 

@@ -75,8 +75,21 @@ typedef struct fwi_config {
     int   hbm_budget_mb;   /* FWI_STORE_AUTO: device memory (MiB) the shot state
                               may take; 0 = 90% of the free memory when
                               fwi_set_shots runs */
-    int   reserved[2];     /* must be zero */
+    int   fd_order;        /* 0 or 4: the reference's staggered 4th order
+                              (fwi_sys.h:7, coefficients fwi_2d.c:304-314);
+                              8: the 8th-order extension (see below) */
+    int   reserved[1];     /* must be zero */
 } fwi_config;
+
+/* The 8th-order extension (fd_order 8; the reference has none).  A staggered
+ * first difference uses the 8th-order stencil
+ *     D+ at position j: sum_k w_k (a[j+k-1] - a[j-k]),   4 <= j <= n-4,
+ *     D- at cell i:     sum_k w_k (b[i+k] - b[i-k+1]),   3 <= i <= n-4,
+ * w = (1225/1024, -245/3072, 49/5120, -5/7168) / h, wherever its 8 points
+ * lie inside the grid, and the reference's formulas of a_lap_opt_2d_pml
+ * (the 4th-order pair, the edge and free-surface rows) elsewhere; the CPML
+ * psi recursions are the reference's.  The rebuild keeps 2M-1 = 7 strips per
+ * side.  The CFL check uses sum |w_k| = 1.2863. */
 
 /* Forward-field storage for the backward half.
  *

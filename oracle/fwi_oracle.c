@@ -53,9 +53,14 @@ typedef struct {
     int nx, nz, npml, fs;
     int pnx, pnz, unx, unz, vnx, vnz;
     int x0, z0;            /* physical origin inside the padded grid */
+    int M;                 /* half the FD order: 2 (the reference's 4th order) or 4 (8th order) */
+    int S;                 /* strip width 2M-1 (fwi_sys.h:7 for M = 2) */
 } grid_t;
 
-typedef struct { float c0x, c1x, ix, c0z, c1z, iz, iz840, iz24; } coe_t;
+typedef struct {
+    float c0x, c1x, ix, c0z, c1z, iz, iz840, iz24;
+    float c8x[4], c8z[4];  /* 8th-order staggered weights / h (fd_order 8) */
+} coe_t;
 
 typedef struct {
     int npml;
@@ -164,6 +169,8 @@ static void make_grid(const orc_config *cfg, grid_t *g)
     g->unx = g->pnx + 1; g->unz = g->pnz;
     g->vnx = g->pnx;     g->vnz = g->pnz + 1;
     g->x0 = cfg->npml;   g->z0 = g->fs ? 0 : cfg->npml;
+    g->M = cfg->fd_order == 8 ? 4 : 2;
+    g->S = 2*g->M - 1;
 }
 
 void orc_grid(const orc_config *cfg, int out[4])
@@ -172,11 +179,26 @@ void orc_grid(const orc_config *cfg, int out[4])
     out[0] = g.pnx; out[1] = g.pnz; out[2] = g.x0; out[3] = g.z0;
 }
 
+/* The 8th-order staggered first-derivative weights (Taylor, M = 4):
+ * f'(x) h = sum_k w_k (f(x + (k - 1/2) h) - f(x - (k - 1/2) h)),
+ * w = 1225/1024, -245/3072, 49/5120, -5/7168, rounded to float after the
+ * division by h (the reference has no 8th-order operator; fwi_sys.h:7). */
+void orc_fd8_coeffs(float dx, float dz, float out[8])
+{
+    static const double w[4] = {1225.0/1024.0, -245.0/3072.0, 49.0/5120.0, -5.0/7168.0};
+    for (int k = 0; k < 4; k++) {
+        out[k]   = (float)(w[k]/(double)dx);
+        out[4+k] = (float)(w[k]/(double)dz);
+    }
+}
+
 static void make_coe(const orc_config *cfg, coe_t *c)
 {
     float o[8]; orc_fd_coeffs(cfg->dx, cfg->dz, o);
     c->c0x = o[0]; c->c1x = o[1]; c->ix = o[2];
     c->c0z = o[3]; c->c1z = o[4]; c->iz = o[5]; c->iz840 = o[6]; c->iz24 = o[7];
+    float w[8]; orc_fd8_coeffs(cfg->dx, cfg->dz, w);
+    for (int k = 0; k < 4; k++) { c->c8x[k] = w[k]; c->c8z[k] = w[4+k]; }
 }
 
 /* CPML profiles, fwi_2d.c:263-283: a0/b0 from cpml_coe, a1/b1 mirrored. */
@@ -402,7 +424,7 @@ static void adjoint_update(real *bnew, const real *bcur, const real *bprev,
 static void write_strips(const grid_t *g, const real *p, real *ud, real *lr)
 {
     const int nx = g->nx, nz = g->nz, pnx = g->pnx, np = g->npml, zo = g->z0;
-    const int S = 3;   /* 2*mm-1 with mm = 2 (fwi_sys.h:7) */
+    const int S = g->S;   /* 2*mm-1, mm = 2 in the reference (fwi_sys.h:7) */
     for (int i = 0; i < S; i++)
         for (int j = 0; j < nx; j++) {
             ud[(size_t)i*nx+j]     = p[(size_t)(i+zo)*pnx + j+np];
@@ -415,10 +437,10 @@ static void write_strips(const grid_t *g, const real *p, real *ud, real *lr)
         }
 }
 
-/* read_bdr, fwi_2d.c:940-957, into the interior-grid field [nz][nx]. */
-static void read_strips(int nx, int nz, const real *ud, const real *lr, real *p)
+/* read_bdr, fwi_2d.c:940-957, into the interior-grid field [nz][nx]; S is
+ * the strip width 2M-1. */
+static void read_strips(int nx, int nz, int S, const real *ud, const real *lr, real *p)
 {
-    const int S = 3;
     for (int i = 0; i < S; i++)
         for (int j = 0; j < nx; j++) {
             p[(size_t)i*nx+j]          = ud[(size_t)i*nx+j];
@@ -561,6 +583,263 @@ static void lap_pml_t(const grid_t *g, const coe_t *c, const pmlc_t *pm, psi_t *
         }
 }
 
+/* ------------------------------------------------------------------------ */
+/* Part 3: the 8th-order extension (fd_order 8, M = 4)                       */
+/* ------------------------------------------------------------------------ */
+/* The reference is 4th order only (MM 2, fwi_sys.h:7).  The 8th-order
+ * operator is defined here, and the GPU engine implements the same
+ * definition: every staggered first difference uses the 8th-order stencil
+ * where its 8 points lie inside the grid, and the reference's own formulas
+ * of a_lap_opt_2d_pml everywhere else (the 4th-order pair, the 2nd-order
+ * edge differences and, with a free surface, the one-sided top rows
+ * fwi_2d.c:805-807 and 848).  The CPML psi recursions are the reference's,
+ * applied to these differences.  Along a line of n cells:
+ *   D+ at position j = 0..n (between cells j-1 and j):
+ *       4 <= j <= n-4: sum_k w_k (a[j+k-1] - a[j-k])
+ *       else the M = 2 rules (fwi_2d.c:775-784, 798-810)
+ *   D- at cell i = 0..n-1 from positions b[0..n]:
+ *       3 <= i <= n-4: sum_k w_k (b[i+k] - b[i-k+1])
+ *       else the M = 2 rules (fwi_2d.c:821-832, 846-855)
+ * The interior operator of the rebuild applies the 8th-order stencil only
+ * (u positions [4, n-4], cells [7, n-7)); the 2M-1 = 7 outer rows and
+ * columns come from the strips.  At those cells the padded operator is the
+ * same stencil, so the rebuild reverses the forward exactly (up to
+ * rounding).  Its exact transpose is written below in scatter form; the
+ * adjoint and finite-difference tests check it. */
+
+#define A8(k) a[(size_t)(k)*st]
+/* D+ at position j of n cells (stride st); top_fs: the free-surface top rows */
+static real dp8(const real *a, size_t st, int n, int j, const float *w, float c0, float c1, float ih, float ih840,
+                int top_fs)
+{
+    if (j >= 4 && j <= n-4)
+        return w[0]*(A8(j) - A8(j-1)) + w[1]*(A8(j+1) - A8(j-2)) + w[2]*(A8(j+2) - A8(j-3)) + w[3]*(A8(j+3) - A8(j-4));
+    if (top_fs && j == 0) return ( 3675.0*A8(0)-1225.0*A8(1)+441.0*A8(2)-75.0*A8(3))*ih840;
+    if (top_fs && j == 1) return (-1085.0*A8(0)+1015.0*A8(1)- 63.0*A8(2) +5.0*A8(3))*ih840;
+    if (j >= 2 && j <= n-2) return c0*(A8(j) - A8(j-1)) + c1*(A8(j+1) - A8(j-2));
+    if (j == 1) return ih*(A8(1) - A8(0));
+    if (j == n-1) return ih*(A8(n-1) - A8(n-2));
+    return 0;
+}
+/* transpose: abar += d(D+ a at j)/da * ybar */
+static void dp8_t(real *a, size_t st, int n, int j, real y, const float *w, float c0, float c1, float ih, float ih840,
+                  int top_fs)
+{
+    if (j >= 4 && j <= n-4) {
+        for (int k = 0; k < 4; k++) { A8(j+k) += w[k]*y; A8(j-1-k) -= w[k]*y; }
+        return;
+    }
+    if (top_fs && j <= 1) {
+        static const double h0[4] = {3675., -1225., 441., -75.}, h1[4] = {-1085., 1015., -63., 5.};
+        for (int k = 0; k < 4; k++) A8(k) += (real)((j == 0 ? h0[k] : h1[k])*y*ih840);
+        return;
+    }
+    if (j >= 2 && j <= n-2) { A8(j) += c0*y; A8(j-1) -= c0*y; A8(j+1) += c1*y; A8(j-2) -= c1*y; return; }
+    if (j == 1) { A8(1) += ih*y; A8(0) -= ih*y; return; }
+    if (j == n-1) { A8(n-1) += ih*y; A8(n-2) -= ih*y; }
+}
+/* D- at cell i from positions b[0..n] */
+static real dm8(const real *a, size_t st, int n, int i, const float *w, float c0, float c1, float ih, float ih24,
+                int top_fs)
+{
+    if (i >= 3 && i <= n-4)
+        return w[0]*(A8(i+1) - A8(i)) + w[1]*(A8(i+2) - A8(i-1)) + w[2]*(A8(i+3) - A8(i-2)) + w[3]*(A8(i+4) - A8(i-3));
+    if (top_fs && i == 0) return (-22.*A8(0)+17.*A8(1)+9.*A8(2)-5.*A8(3)+A8(4))*ih24;
+    if (i >= 1 && i <= n-2) return c0*(A8(i+1) - A8(i)) + c1*(A8(i+2) - A8(i-1));
+    if (i == 0) return (A8(1) - A8(0))*ih;
+    return (A8(n) - A8(n-1))*ih;
+}
+static void dm8_t(real *a, size_t st, int n, int i, real y, const float *w, float c0, float c1, float ih, float ih24,
+                  int top_fs)
+{
+    if (i >= 3 && i <= n-4) {
+        for (int k = 0; k < 4; k++) { A8(i+1+k) += w[k]*y; A8(i-k) -= w[k]*y; }
+        return;
+    }
+    if (top_fs && i == 0) {
+        static const double h[5] = {-22., 17., 9., -5., 1.};
+        for (int k = 0; k < 5; k++) A8(k) += (real)(h[k]*y*ih24);
+        return;
+    }
+    if (i >= 1 && i <= n-2) { A8(i+1) += c0*y; A8(i) -= c0*y; A8(i+2) += c1*y; A8(i-1) -= c1*y; return; }
+    if (i == 0) { A8(1) += ih*y; A8(0) -= ih*y; return; }
+    A8(n) += ih*y; A8(n-1) -= ih*y;
+}
+#undef A8
+
+/* The 8th-order CPML operator, the counterpart of lap_pml. */
+static void lap_pml8(const grid_t *g, const coe_t *c, const pmlc_t *pm, psi_t *s,
+                     const real *p, real *u, real *v, real *ux, real *vz)
+{
+    const int pnx = g->pnx, pnz = g->pnz, unx = g->unx, unz = g->unz;
+    const int vnx = g->vnx, vnz = g->vnz, np = g->npml, un1 = np+1, fs = g->fs;
+    #pragma omp parallel for
+    for (int iz = 0; iz < unz; iz++)
+        for (int j = 0; j < unx; j++)
+            u[(size_t)iz*unx+j] = dp8(p + (size_t)iz*pnx, 1, pnx, j, c->c8x, c->c0x, c->c1x, c->ix, 0.f, 0);
+    #pragma omp parallel for
+    for (int iz = 0; iz < unz; iz++)
+        for (int ix = 0; ix < np+1; ix++) {
+            real *q0 = &s->u0[(size_t)iz*un1+ix], *q1 = &s->u1[(size_t)iz*un1+ix];
+            real *a0 = &u[(size_t)iz*unx+ix], *a1 = &u[(size_t)iz*unx+ix+unx-np-1];
+            *q0 = pm->b0[0][2*ix]*(*q0) + pm->a0[0][2*ix]*(*a0);
+            *a0 += *q0;
+            *q1 = pm->b1[0][2*ix]*(*q1) + pm->a1[0][2*ix]*(*a1);
+            *a1 += *q1;
+        }
+    #pragma omp parallel for
+    for (int kv = 0; kv < vnz; kv++)
+        for (int ix = 0; ix < vnx; ix++)
+            v[(size_t)kv*vnx+ix] = dp8(p + ix, pnx, pnz, kv, c->c8z, c->c0z, c->c1z, c->iz, c->iz840, fs);
+    #pragma omp parallel for
+    for (int iz = 0; iz < np+1; iz++)
+        for (int ix = 0; ix < vnx; ix++) {
+            if (!fs) {
+                real *q0 = &s->v0[(size_t)iz*vnx+ix], *a0 = &v[(size_t)iz*vnx+ix];
+                *q0 = pm->b0[1][2*iz]*(*q0) + pm->a0[1][2*iz]*(*a0);
+                *a0 += *q0;
+            }
+            real *q1 = &s->v1[(size_t)iz*vnx+ix], *a1 = &v[(size_t)(iz+vnz-np-1)*vnx+ix];
+            *q1 = pm->b1[1][2*iz]*(*q1) + pm->a1[1][2*iz]*(*a1);
+            *a1 += *q1;
+        }
+    #pragma omp parallel for
+    for (int iz = 0; iz < pnz; iz++)
+        for (int i = 0; i < pnx; i++)
+            ux[(size_t)iz*pnx+i] = dm8(u + (size_t)iz*unx, 1, pnx, i, c->c8x, c->c0x, c->c1x, c->ix, 0.f, 0);
+    #pragma omp parallel for
+    for (int iz = 0; iz < pnz; iz++)
+        for (int ix = 0; ix < np; ix++) {
+            real *q0 = &s->ux0[(size_t)iz*np+ix], *q1 = &s->ux1[(size_t)iz*np+ix];
+            real *a0 = &ux[(size_t)iz*pnx+ix], *a1 = &ux[(size_t)iz*pnx+ix+pnx-np];
+            *q0 = pm->b0[0][2*ix+1]*(*q0) + pm->a0[0][2*ix+1]*(*a0);
+            *a0 += *q0;
+            *q1 = pm->b1[0][2*ix+1]*(*q1) + pm->a1[0][2*ix+1]*(*a1);
+            *a1 += *q1;
+        }
+    #pragma omp parallel for
+    for (int k = 0; k < pnz; k++)
+        for (int ix = 0; ix < pnx; ix++)
+            vz[(size_t)k*pnx+ix] = dm8(v + ix, vnx, pnz, k, c->c8z, c->c0z, c->c1z, c->iz, c->iz24, fs);
+    #pragma omp parallel for
+    for (int iz = 0; iz < np; iz++)
+        for (int ix = 0; ix < pnx; ix++) {
+            if (!fs) {
+                real *q0 = &s->vz0[(size_t)iz*pnx+ix], *a0 = &vz[(size_t)iz*pnx+ix];
+                *q0 = pm->b0[1][2*iz+1]*(*q0) + pm->a0[1][2*iz+1]*(*a0);
+                *a0 += *q0;
+            }
+            real *q1 = &s->vz1[(size_t)iz*pnx+ix], *a1 = &vz[(size_t)(iz+pnz-np)*pnx+ix];
+            *q1 = pm->b1[1][2*iz+1]*(*q1) + pm->a1[1][2*iz+1]*(*a1);
+            *a1 += *q1;
+        }
+}
+
+/* psi transpose of one site: y = x + psi', psi' = b psi + a x, carried
+ * cotangent cc: t = ybar + cc; xbar = ybar + a t; cc = b t. */
+static inline real psi_t1(real y, real *cc, float a, float b)
+{
+    real t = y + *cc;
+    *cc = b*t;
+    return y + a*t;
+}
+
+/* Exact transpose of lap_pml8 (scatter form, one row or column per thread). */
+static void lap_pml8_t(const grid_t *g, const coe_t *c, const pmlc_t *pm, psi_t *s,
+                       const real *q, real *pbar, real *rx, real *ub, real *rz, real *vb)
+{
+    const int pnx = g->pnx, pnz = g->pnz, unx = g->unx, vnx = g->vnx, vnz = g->vnz;
+    const int np = g->npml, un1 = np+1, fs = g->fs;
+    #pragma omp parallel for
+    for (int iz = 0; iz < pnz; iz++) {
+        real *r = rx + (size_t)iz*pnx, *b = ub + (size_t)iz*unx, *pb = pbar + (size_t)iz*pnx;
+        for (int i = 0; i < pnx; i++) r[i] = q[(size_t)iz*pnx+i];
+        for (int ix = 0; ix < np; ix++) {
+            r[ix+pnx-np] = psi_t1(r[ix+pnx-np], &s->ux1[(size_t)iz*np+ix], pm->a1[0][2*ix+1], pm->b1[0][2*ix+1]);
+            r[ix] = psi_t1(r[ix], &s->ux0[(size_t)iz*np+ix], pm->a0[0][2*ix+1], pm->b0[0][2*ix+1]);
+        }
+        for (int j = 0; j < unx; j++) b[j] = 0;
+        for (int i = 0; i < pnx; i++) dm8_t(b, 1, pnx, i, r[i], c->c8x, c->c0x, c->c1x, c->ix, 0.f, 0);
+        for (int ix = 0; ix < np+1; ix++) {
+            b[ix+unx-np-1] = psi_t1(b[ix+unx-np-1], &s->u1[(size_t)iz*un1+ix], pm->a1[0][2*ix], pm->b1[0][2*ix]);
+            b[ix] = psi_t1(b[ix], &s->u0[(size_t)iz*un1+ix], pm->a0[0][2*ix], pm->b0[0][2*ix]);
+        }
+        for (int i = 0; i < pnx; i++) pb[i] = 0;
+        for (int j = 0; j < unx; j++) dp8_t(pb, 1, pnx, j, b[j], c->c8x, c->c0x, c->c1x, c->ix, 0.f, 0);
+    }
+    #pragma omp parallel for
+    for (int ix = 0; ix < pnx; ix++) {
+        for (int k = 0; k < pnz; k++) {
+            real val = q[(size_t)k*pnx+ix];
+            if (k >= pnz-np) { int kk = k-(pnz-np); val = psi_t1(val, &s->vz1[(size_t)kk*pnx+ix], pm->a1[1][2*kk+1], pm->b1[1][2*kk+1]); }
+            if (!fs && k < np) val = psi_t1(val, &s->vz0[(size_t)k*pnx+ix], pm->a0[1][2*k+1], pm->b0[1][2*k+1]);
+            rz[(size_t)k*pnx+ix] = val;
+        }
+        for (int kv = 0; kv < vnz; kv++) vb[(size_t)kv*vnx+ix] = 0;
+        for (int k = 0; k < pnz; k++)
+            dm8_t(vb + ix, vnx, pnz, k, rz[(size_t)k*pnx+ix], c->c8z, c->c0z, c->c1z, c->iz, c->iz24, fs);
+        for (int kv = 0; kv < vnz; kv++) {
+            real *o = &vb[(size_t)kv*vnx+ix];
+            if (kv >= vnz-np-1) { int kk = kv-(vnz-np-1); *o = psi_t1(*o, &s->v1[(size_t)kk*vnx+ix], pm->a1[1][2*kk], pm->b1[1][2*kk]); }
+            if (!fs && kv <= np) *o = psi_t1(*o, &s->v0[(size_t)kv*vnx+ix], pm->a0[1][2*kv], pm->b0[1][2*kv]);
+        }
+        for (int kv = 0; kv < vnz; kv++)
+            dp8_t(pbar + ix, pnx, pnz, kv, vb[(size_t)kv*vnx+ix], c->c8z, c->c0z, c->c1z, c->iz, c->iz840, fs);
+    }
+}
+
+/* The 8th-order interior operator of the rebuild on [nz][nx]: u positions
+ * [4, nx-4], v positions [4, nz-4], ux/vz cells [7, n-7). */
+static void lap_int8(int nx, int nz, const coe_t *c, const real *p, real *u, real *v, real *ux, real *vz)
+{
+    const int unx = nx+1;
+    const float *wx = c->c8x, *wz = c->c8z;
+    #pragma omp parallel for
+    for (int iz = 0; iz < nz; iz++)
+        for (int j = 4; j <= nx-4; j++) {
+            const real *a = p + (size_t)iz*nx;
+            u[(size_t)iz*unx+j] = wx[0]*(a[j]-a[j-1]) + wx[1]*(a[j+1]-a[j-2]) + wx[2]*(a[j+2]-a[j-3]) + wx[3]*(a[j+3]-a[j-4]);
+        }
+    #pragma omp parallel for
+    for (int kv = 4; kv <= nz-4; kv++)
+        for (int ix = 0; ix < nx; ix++) {
+#define PA(k) p[(size_t)(k)*nx+ix]
+            v[(size_t)kv*nx+ix] = wz[0]*(PA(kv)-PA(kv-1)) + wz[1]*(PA(kv+1)-PA(kv-2)) + wz[2]*(PA(kv+2)-PA(kv-3)) +
+                                  wz[3]*(PA(kv+3)-PA(kv-4));
+#undef PA
+        }
+    #pragma omp parallel for
+    for (int iz = 7; iz < nz-7; iz++)
+        for (int i = 7; i < nx-7; i++) {
+            const real *b = u + (size_t)iz*unx;
+            ux[(size_t)iz*nx+i] = wx[0]*(b[i+1]-b[i]) + wx[1]*(b[i+2]-b[i-1]) + wx[2]*(b[i+3]-b[i-2]) + wx[3]*(b[i+4]-b[i-3]);
+        }
+    #pragma omp parallel for
+    for (int k = 7; k < nz-7; k++)
+        for (int ix = 0; ix < nx; ix++) {
+#define VA(kk) v[(size_t)(kk)*nx+ix]
+            vz[(size_t)k*nx+ix] = wz[0]*(VA(k+1)-VA(k)) + wz[1]*(VA(k+2)-VA(k-1)) + wz[2]*(VA(k+3)-VA(k-2)) +
+                                  wz[3]*(VA(k+4)-VA(k-3));
+#undef VA
+        }
+}
+
+/* Operator selection by the FD order. */
+static void lap_op(const grid_t *g, const coe_t *c, const pmlc_t *pm, psi_t *s,
+                   const real *p, real *u, real *v, real *ux, real *vz)
+{
+    if (g->M == 4) lap_pml8(g, c, pm, s, p, u, v, ux, vz); else lap_pml(g, c, pm, s, p, u, v, ux, vz);
+}
+static void lap_op_t(const grid_t *g, const coe_t *c, const pmlc_t *pm, psi_t *s,
+                     const real *q, real *pbar, real *rx, real *ub, real *rz, real *vb)
+{
+    if (g->M == 4) lap_pml8_t(g, c, pm, s, q, pbar, rx, ub, rz, vb); else lap_pml_t(g, c, pm, s, q, pbar, rx, ub, rz, vb);
+}
+static void lap_int_op(const grid_t *g, const coe_t *c, const real *p, real *u, real *v, real *ux, real *vz)
+{
+    if (g->M == 4) lap_int8(g->nx, g->nz, c, p, u, v, ux, vz); else lap_int(g->nx, g->nz, c, p, u, v, ux, vz);
+}
+
 typedef struct {
     orc_config cfg;
     grid_t g;
@@ -632,9 +911,9 @@ static int run_forward(const orc_ctx *x, const orc_shot *sh, real *syn,
     real *u = blk+5*np2, *v = u+nu;
     psi_t s; psi_bind(g, v+nv, &s);
     const size_t isrc = (size_t)(sh->isz+g->z0)*g->pnx + sh->isx+g->x0;
-    const size_t udn = (size_t)6*g->nx, lrn = (size_t)6*g->nz;
+    const size_t udn = (size_t)2*g->S*g->nx, lrn = (size_t)2*g->S*g->nz;
     for (int it = 0; it < x->cfg.nt; it++) {
-        lap_pml(g, &x->c, &x->pm, &s, pnow, u, v, ux, vz);
+        lap_op(g, &x->c, &x->pm, &s, pnow, u, v, ux, vz);
         time_integral(pnew, pnow, pold, ux, vz, x->ekp, g->pnz, g->pnx, g->pnx);
         real amp = (real)sh->wav[it]*(real)x->iarea;
         pnew[isrc] += amp*(real)x->ekp[isrc];
@@ -688,12 +967,13 @@ static int run_backward(const orc_ctx *x, const orc_shot *sh, const real *res,
         }
     const size_t isrc = (size_t)(sh->isz+g->z0)*pnx + sh->isx+g->x0;
     const size_t isrc_i = (size_t)sh->isz*nx + sh->isx;
-    const int src_interior = sh->isz >= 3 && sh->isz < nz-3 && sh->isx >= 3 && sh->isx < nx-3;
-    const size_t udn = (size_t)6*nx, lrn = (size_t)6*nz;
+    const int S = g->S;
+    const int src_interior = sh->isz >= S && sh->isz < nz-S && sh->isx >= S && sh->isx < nx-S;
+    const size_t udn = (size_t)2*S*nx, lrn = (size_t)2*S*nz;
     const int jump = x->cfg.jump;
     for (int m = x->cfg.nt; m >= 1; m--) {
         /* adjoint step: b^m = 2 b^{m+1} - b^{m+2} + K (L^T b^{m+1} + r^m) */
-        lap_pml_t(g, &x->c, &x->pm, &s, bcur, pbar, rx, ub, rz, vb);
+        lap_op_t(g, &x->c, &x->pm, &s, bcur, pbar, rx, ub, rz, vb);
         if ((m-1) % jump == 0) {
             int k = (m-1)/jump;
             for (int r = 0; r < sh->nr; r++)
@@ -702,17 +982,17 @@ static int run_backward(const orc_ctx *x, const orc_shot *sh, const real *res,
         adjoint_update(bnew, bcur, bprev, pbar, x->ekp, np2);
         if (wbar) wbar[m-1] = (real)x->iarea*bnew[isrc];
         /* source-field rebuild: p^{m-2} */
-        lap_int(nx, nz, &x->c, rp_cur, ru, rv, rux, rvz);
+        lap_int_op(g, &x->c, rp_cur, ru, rv, rux, rvz);
         time_integral(rp_new, rp_cur, rp_prev, rux, rvz, ekpi, nz, nx, nx);
         real fsrc = (real)sh->wav[m-1]*(real)x->iarea;
         rp_new[isrc_i] += fsrc*(real)ekpi[isrc_i];
         if (m-2 >= 1) {
-            read_strips(nx, nz, ring_ud + (size_t)(m-3)*udn, ring_lr + (size_t)(m-3)*lrn, rp_new);
+            read_strips(nx, nz, S, ring_ud + (size_t)(m-3)*udn, ring_lr + (size_t)(m-3)*lrn, rp_new);
         } else {
-            for (int i = 0; i < 3; i++)
+            for (int i = 0; i < S; i++)
                 for (int j = 0; j < nx; j++) { rp_new[(size_t)i*nx+j] = 0; rp_new[(size_t)(nz-1-i)*nx+j] = 0; }
             for (int i = 0; i < nz; i++)
-                for (int j = 0; j < 3; j++) { rp_new[(size_t)i*nx+j] = 0; rp_new[(size_t)i*nx+nx-1-j] = 0; }
+                for (int j = 0; j < S; j++) { rp_new[(size_t)i*nx+j] = 0; rp_new[(size_t)i*nx+nx-1-j] = 0; }
         }
         for (int i = 0; i < nsnap; i++)
             if (steps[i] == m-2) memcpy(snaps + (size_t)i*ni, rp_new, ni*sizeof(real));
@@ -722,7 +1002,7 @@ static int run_backward(const orc_ctx *x, const orc_shot *sh, const real *res,
             for (int ix = 0; ix < nx; ix++) {
                 size_t o = (size_t)iz*nx+ix;
                 real lp;
-                if (iz >= 3 && iz < nz-3 && ix >= 3 && ix < nx-3) {
+                if (iz >= S && iz < nz-S && ix >= S && ix < nx-S) {
                     lp = rux[o] + rvz[o];
                     if (src_interior && o == isrc_i) lp += fsrc;
                 } else {
@@ -748,7 +1028,7 @@ int orc_apply_op(const orc_config *cfg, const REAL_T *p, REAL_T *psi, REAL_T *w)
     real *blk = (real *)calloc(2*np2 + nu + nv, sizeof(real));
     if (!blk) { free_pmlc(&pm); return ORC_ERR_NOMEM; }
     psi_t s; psi_bind(&g, psi, &s);
-    lap_pml(&g, &c, &pm, &s, p, blk+2*np2, blk+2*np2+nu, blk, blk+np2);
+    lap_op(&g, &c, &pm, &s, p, blk+2*np2, blk+2*np2+nu, blk, blk+np2);
     for (size_t i = 0; i < np2; i++) w[i] = blk[i] + blk[np2+i];
     free(blk); free_pmlc(&pm);
     return ORC_OK;
@@ -764,7 +1044,7 @@ int orc_apply_op_t(const orc_config *cfg, const REAL_T *q, REAL_T *psib, REAL_T 
     real *blk = (real *)calloc(2*np2 + nu + nv, sizeof(real));
     if (!blk) { free_pmlc(&pm); return ORC_ERR_NOMEM; }
     psi_t s; psi_bind(&g, psib, &s);
-    lap_pml_t(&g, &c, &pm, &s, q, pbar, blk, blk+2*np2, blk+np2, blk+2*np2+nu);
+    lap_op_t(&g, &c, &pm, &s, q, pbar, blk, blk+2*np2, blk+np2, blk+2*np2+nu);
     free(blk); free_pmlc(&pm);
     return ORC_OK;
 }
@@ -788,8 +1068,8 @@ static int shot_gradient(const orc_ctx *x, const orc_shot *sh, const float *obs,
     const size_t np2 = (size_t)g->pnx*g->pnz;
     const size_t nrt = (size_t)sh->nr*x->nt0;
     const size_t nt = (size_t)x->cfg.nt;
-    real *ud = (real *)malloc(nt*6*(size_t)g->nx*sizeof(real));
-    real *lr = (real *)malloc(nt*6*(size_t)g->nz*sizeof(real));
+    real *ud = (real *)malloc(nt*2*g->S*(size_t)g->nx*sizeof(real));
+    real *lr = (real *)malloc(nt*2*g->S*(size_t)g->nz*sizeof(real));
     real *pf = (real *)malloc(2*np2*sizeof(real));
     real *syn = (real *)calloc(nrt ? nrt : 1, sizeof(real));
     real *res = (real *)calloc(nrt ? nrt : 1, sizeof(real));
@@ -878,8 +1158,8 @@ int orc_probe(const orc_config *cfg, const float *vel, const orc_shot *shot,
     const grid_t *g = &x.g;
     const size_t np2 = (size_t)g->pnx*g->pnz, ni = (size_t)g->nx*g->nz;
     const size_t nt = (size_t)cfg->nt, nrt = (size_t)shot->nr*x.nt0;
-    real *ud = (real *)malloc(nt*6*(size_t)g->nx*sizeof(real));
-    real *lr = (real *)malloc(nt*6*(size_t)g->nz*sizeof(real));
+    real *ud = (real *)malloc(nt*2*g->S*(size_t)g->nx*sizeof(real));
+    real *lr = (real *)malloc(nt*2*g->S*(size_t)g->nz*sizeof(real));
     real *pf = (real *)malloc(2*np2*sizeof(real));
     real *res = (real *)calloc(nrt ? nrt : 1, sizeof(real));
     real *gacc = (real *)calloc(ni, sizeof(real));
@@ -902,17 +1182,19 @@ int orc_strips_write(const orc_config *cfg, const REAL_T *p, REAL_T *ud, REAL_T 
 
 int orc_strips_read(const orc_config *cfg, const REAL_T *ud, const REAL_T *lr, REAL_T *p)
 {
-    read_strips(cfg->nx, cfg->nz, ud, lr, p);
+    grid_t g; make_grid(cfg, &g);
+    read_strips(cfg->nx, cfg->nz, g.S, ud, lr, p);
     return ORC_OK;
 }
 
 int orc_apply_int(const orc_config *cfg, const REAL_T *p, REAL_T *ux, REAL_T *vz)
 {
     coe_t c; make_coe(cfg, &c);
+    grid_t g; make_grid(cfg, &g);
     const size_t nu = (size_t)(cfg->nx+1)*cfg->nz, nv = (size_t)cfg->nx*(cfg->nz+1);
     real *blk = (real *)calloc(nu+nv, sizeof(real));
     if (!blk) return ORC_ERR_NOMEM;
-    lap_int(cfg->nx, cfg->nz, &c, p, blk, blk+nu, ux, vz);
+    lap_int_op(&g, &c, p, blk, blk+nu, ux, vz);
     free(blk);
     return ORC_OK;
 }

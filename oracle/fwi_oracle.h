@@ -42,6 +42,8 @@ typedef struct {
     float pml_max_v;     /* MAX_V  (fwi_sys.h:3) */
     float pml_coef_r;    /* COEF_R (fwi_sys.h:4) */
     int nthreads;        /* OpenMP threads; <= 0 keeps the runtime default */
+    int fd_order;        /* 4 (or 0): the reference's staggered 4th order (M = 2);
+                            8: the 8th-order extension (M = 4, strips of 2M-1 = 7) */
 } orc_config;
 
 typedef struct {
@@ -70,6 +72,9 @@ void orc_model_ext(const float *model, int n1, int n2, float *emodel, int en1, i
 /* FD coefficients as fwi_2d.c:304-314 computes them:
  * out = {c0x, c1x, ix, c0z, c1z, iz, iz840, iz24}. */
 void orc_fd_coeffs(float dx, float dz, float out[8]);
+
+/* 8th-order staggered weights / h: out = {w1..w4 / dx, w1..w4 / dz}. */
+void orc_fd8_coeffs(float dx, float dz, float out[8]);
 
 /* Cell (ix, iz) of a position (x, z) in metres, as fwi_2d.c:363-364. */
 void orc_cell_of(float x, float z, float dx, float dz, int *ix, int *iz);

@@ -28,7 +28,7 @@ class OrcConfig(C.Structure):
                 ("free_surface", C.c_int), ("nt", C.c_int), ("jump", C.c_int),
                 ("dx", C.c_float), ("dz", C.c_float), ("dt", C.c_float),
                 ("pml_max_f", C.c_float), ("pml_max_v", C.c_float),
-                ("pml_coef_r", C.c_float), ("nthreads", C.c_int)]
+                ("pml_coef_r", C.c_float), ("nthreads", C.c_int), ("fd_order", C.c_int)]
 
 
 class OrcShot(C.Structure):
@@ -62,10 +62,11 @@ def _ptr(a, ctype):
 
 
 def make_config(nx, nz, npml, nt, dx, dz, dt, free_surface=1, jump=1,
-                pml_max_f=15.0, pml_max_v=6000.0, pml_coef_r=0.001, nthreads=0) -> OrcConfig:
-    """Defaults of the CPML constants are fwi_sys.h:2-4 (MAX_F, MAX_V, COEF_R)."""
+                pml_max_f=15.0, pml_max_v=6000.0, pml_coef_r=0.001, nthreads=0, fd_order=4) -> OrcConfig:
+    """Defaults of the CPML constants are fwi_sys.h:2-4 (MAX_F, MAX_V, COEF_R);
+    fd_order 4 is the reference's (fwi_sys.h:7), 8 the 8th-order extension."""
     return OrcConfig(nx, nz, npml, int(free_surface), nt, jump, dx, dz, dt,
-                     pml_max_f, pml_max_v, pml_coef_r, nthreads)
+                     pml_max_f, pml_max_v, pml_coef_r, nthreads, fd_order)
 
 
 class Shot:
@@ -168,9 +169,10 @@ class Oracle:
         return ux, vz
 
     def strips_write(self, cfg, p_pad):
+        S = 7 if cfg.fd_order == 8 else 3
         p_pad = np.ascontiguousarray(p_pad, self.real)
-        ud = np.zeros((6, cfg.nx), self.real)
-        lr = np.zeros((cfg.nz, 6), self.real)
+        ud = np.zeros((2 * S, cfg.nx), self.real)
+        lr = np.zeros((cfg.nz, 2 * S), self.real)
         self.lib.orc_strips_write(C.byref(cfg), _ptr(p_pad, self.creal), _ptr(ud, self.creal),
                                   _ptr(lr, self.creal))
         return ud, lr

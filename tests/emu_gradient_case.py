@@ -1,8 +1,8 @@
 """One gradient through the CPU emulation build of the engine, checked
 against the FP64 oracle; run by test_emu_sanitized.py in a child process
 with AddressSanitizer and UBSan preloaded and FWI_LIB pointing at
-libfwiemu.so.  Prints one JSON line {J, J64, grad_rel, syn_rel}.  With a
-fifth argument nseg > 0 the same gradient is also taken with checkpoints
+libfwiemu.so.  Arguments: free surface, nt, nx, nz [, nseg [, fd_order]].
+Prints one JSON line {J, J64, grad_rel, syn_rel}.  With nseg > 0 the same gradient is also taken with checkpoints
 (FWI_STORE_SNAPSHOTS, nseg segments) in FP32 and FP16 storage (BF16 shares
 the FP16 path but for its rounding) and the line adds {snap_f32_rel,
 snap_f16_rel} (against FP64) and snap_f32_vs_strips."""
@@ -21,9 +21,9 @@ import oracle as O                         # noqa: E402
 from test_gpu_parity import Case, rel      # noqa: E402
 
 
-def main(fs, nt, nx=150, nz=90, nseg=0):
+def main(fs, nt, nx=150, nz=90, nseg=0, order=4):
     o64 = O.Oracle("f64")
-    case = Case(O, fs, seed=11 + fs, nt=nt, nx=nx, nz=nz)
+    case = Case(O, fs, seed=11 + fs, nt=nt, nx=nx, nz=nz, order=order)
     case.vtrue = (case.vel * 1.08).astype(np.float32)    # signal in the direct waves of a short record
     obs = case.oracle_obs(o64)
     e = case.engine()
@@ -46,7 +46,7 @@ def main(fs, nt, nx=150, nz=90, nseg=0):
             c = case.ecfg
             cfg = fwigpu.make_config(c.nx, c.nz, c.dx, c.dz, c.dt, c.nt_max, npml=c.npml,
                                      free_surface=c.free_surface, jump=c.jump, store=fwigpu.STORE_SNAPSHOTS,
-                                     snapshots=nseg, snap_precision=prec)
+                                     snapshots=nseg, snap_precision=prec, fd_order=c.fd_order)
             with fwigpu.Engine(cfg) as es:
                 es.set_shots(case.eshots)
                 es.set_model(case.vel)

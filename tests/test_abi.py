@@ -55,16 +55,16 @@ def test_check_config_rejects_bad_input(engine_lib):
     assert fwigpu.check_config(good) == 0
     for field, val in [("nx", 4), ("npml", 0), ("dt", 0.0), ("jump", 0), ("free_surface", 2),
                        ("pml_coef_r", 1.5), ("nt_max", 0), ("store", 3), ("store", -1), ("snapshots", -2),
-                       ("snap_precision", 3), ("hbm_budget_mb", -1)]:
+                       ("snap_precision", 3), ("hbm_budget_mb", -1), ("fd_order", 6), ("fd_order", 2)]:
         cfg = fwigpu.make_config(64, 48, 10.0, 10.0, 0.001, 100)
         setattr(cfg, field, val)
         assert fwigpu.check_config(cfg) == -1, field
     cfg = fwigpu.make_config(64, 48, 10.0, 10.0, 0.001, 100)
-    cfg.reserved[1] = 1
+    cfg.reserved[0] = 1
     assert fwigpu.check_config(cfg) == -1
-    for store, prec in [(2, 0), (2, 1), (2, 2), (1, 0), (0, 2)]:
+    for store, prec, order in [(2, 0, 4), (2, 1, 8), (2, 2, 0), (1, 0, 8), (0, 2, 4)]:
         assert fwigpu.check_config(fwigpu.make_config(64, 48, 10.0, 10.0, 0.001, 100, store=store,
-                                                      snap_precision=prec)) == 0
+                                                      snap_precision=prec, fd_order=order)) == 0
 
 
 def test_create_without_device_reports_nodevice(engine_lib):

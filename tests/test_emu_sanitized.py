@@ -51,7 +51,7 @@ def test_emulated_gradient_is_memory_safe_and_matches_oracle(emu_lib, oracles, f
     lib, libs = emu_lib
     env = dict(os.environ, FWI_LIB=lib, LD_PRELOAD=" ".join(libs),
                ASAN_OPTIONS="detect_leaks=0:abort_on_error=1", UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1")
-    r = subprocess.run([sys.executable, os.path.join(HERE, "emu_gradient_case.py"), str(fs), "61", str(nx), str(nz)],
+    r = subprocess.run([sys.executable, os.path.join(HERE, "emu_gradient_case.py"), str(fs), "41", str(nx), str(nz)],
                        capture_output=True, text=True, env=env, timeout=900)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-6000:]
     assert "ERROR: AddressSanitizer" not in r.stderr and "runtime error" not in r.stderr, r.stderr[-6000:]
@@ -81,6 +81,24 @@ def test_emulated_checkpointing_is_memory_safe(emu_lib, oracles):
     assert out["grad_rel"] <= GRAD_TOL, out
     assert out["snap_f32_rel"] <= GRAD_TOL and out["snap_f32_vs_strips"] <= 1e-5, out
     assert out["snap_f16_rel"] <= 1e-3, out
+
+
+def test_emulated_eighth_order_is_memory_safe(emu_lib, oracles):
+    """The 8th-order kernels (fwi_kernels8.cuh) with CPML on all four sides,
+    strips of 7 and the checkpointed backward in 5 segments: memory safe,
+    seismograms and gradient within the parity tolerances of the 8th-order
+    FP64 oracle, FP32 checkpoints within rounding of the strip ring."""
+    lib, libs = emu_lib
+    env = dict(os.environ, FWI_LIB=lib, LD_PRELOAD=" ".join(libs),
+               ASAN_OPTIONS="detect_leaks=0:abort_on_error=1", UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1")
+    r = subprocess.run([sys.executable, os.path.join(HERE, "emu_gradient_case.py"), "0", "41", "130", "70", "5", "8"],
+                       capture_output=True, text=True, env=env, timeout=1200)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-6000:]
+    assert "ERROR: AddressSanitizer" not in r.stderr and "runtime error" not in r.stderr, r.stderr[-6000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["syn_rel"] <= SYN_TOL and abs(out["J"] - out["J64"]) <= 1e-5 * out["J64"], out
+    assert out["grad_rel"] <= GRAD_TOL and out["snap_f32_rel"] <= GRAD_TOL, out
+    assert out["snap_f32_vs_strips"] <= 1e-5 and out["snap_f16_rel"] <= 1e-3, out
 
 
 def test_emulated_aux_routines_are_memory_safe_and_match_oracle(emu_lib, oracles):

@@ -29,7 +29,7 @@ class Case:
     the engine (metres, converted by fwi_2d.c:363-371's rounding)."""
 
     def __init__(self, O, fs, nx=150, nz=90, npml=10, nt=301, jump=2, dx=10.0, dz=10.0, dt=0.001, seed=0,
-                 shots=None):
+                 shots=None, order=4):
         import fwigpu
         self.O, self.fs = O, fs
         self.dx, self.dz = dx, dz
@@ -38,7 +38,9 @@ class Case:
         self.vel = (0.5 * self.vel + 0.5 * np.linspace(1600, 3000, nz)[:, None]).astype(np.float32)
         self.vtrue = self.vel.copy()
         self.vtrue[nz // 6:nz // 6 + 10, nx // 4:3 * nx // 4] += 250.0
-        self.ocfg = O.make_config(nx=nx, nz=nz, npml=npml, nt=nt, dx=dx, dz=dz, dt=dt, free_surface=fs, jump=jump)
+        self.order = order
+        self.ocfg = O.make_config(nx=nx, nz=nz, npml=npml, nt=nt, dx=dx, dz=dz, dt=dt, free_surface=fs, jump=jump,
+                                  fd_order=order)
         self.shot_specs = shots or self.default_shots(rng, nx, nz, nt, jump, dt)
         self.oshots = []
         self.eshots = []
@@ -47,7 +49,8 @@ class Case:
             rec = np.stack([np.asarray(irx) * dx + 0.1 * dx, np.asarray(irz) * dz + 0.4 * dz], axis=1)
             self.eshots.append(fwigpu.ShotSpec(isx * dx + 0.1 * dx, isz * dz + 0.4 * dz, rec, wav))
         nt_max = max(len(s[4]) for s in self.shot_specs)
-        self.ecfg = fwigpu.make_config(nx, nz, dx, dz, dt, nt_max, npml=npml, free_surface=fs, jump=jump)
+        self.ecfg = fwigpu.make_config(nx, nz, dx, dz, dt, nt_max, npml=npml, free_surface=fs, jump=jump,
+                                       fd_order=order)
 
     @staticmethod
     def default_shots(rng, nx, nz, nt, jump, dt):
@@ -70,7 +73,7 @@ class Case:
         O = self.O
         c = self.ocfg
         return O.make_config(nx=c.nx, nz=c.nz, npml=c.npml, nt=nt, dx=c.dx, dz=c.dz, dt=c.dt,
-                             free_surface=c.free_surface, jump=c.jump)
+                             free_surface=c.free_surface, jump=c.jump, fd_order=c.fd_order)
 
     def engine(self):
         import fwigpu

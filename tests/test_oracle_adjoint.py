@@ -1,5 +1,7 @@
 """Pins the oracle's gradient definition (the reference has none: grad4_1shot
-is declared at header.h:283 but never defined).
+is declared at header.h:283 but never defined), for the reference's 4th
+order and for the 8th-order extension (which the reference lacks, so these
+tests are its only pin):
 
 * transpose test of one CPML operator step with its psi memory, over several
   steps: <L x, y> == <x, L^T y> in FP64;
@@ -14,8 +16,12 @@ import pytest
 from conftest import ricker
 
 
-def small_cfg(O, fs, nt=401, jump=2):
-    return O.make_config(nx=40, nz=36, npml=8, nt=nt, dx=10.0, dz=10.0, dt=0.001, free_surface=fs, jump=jump)
+ORDERS = [(1, 4), (0, 4), (1, 8), (0, 8)]
+
+
+def small_cfg(O, fs, nt=401, jump=2, order=4):
+    return O.make_config(nx=40, nz=36, npml=8, nt=nt, dx=10.0, dz=10.0, dt=0.001, free_surface=fs, jump=jump,
+                         fd_order=order)
 
 
 def geometry(O, fs, wav):
@@ -25,10 +31,10 @@ def geometry(O, fs, wav):
     return O.Shot(17, 2, irx, irz, wav)
 
 
-@pytest.mark.parametrize("fs", [1, 0])
-def test_operator_transpose(oracles, fs):
+@pytest.mark.parametrize("fs,order", ORDERS)
+def test_operator_transpose(oracles, fs, order):
     O, _, o64 = oracles
-    cfg = small_cfg(O, fs)
+    cfg = small_cfg(O, fs, order=order)
     pnx, pnz, _, _ = o64.grid(cfg)
     rng = np.random.default_rng(11 + fs)
     n = o64.psi_len(cfg)
@@ -46,10 +52,10 @@ def test_operator_transpose(oracles, fs):
     assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
 
 
-@pytest.mark.parametrize("fs", [1, 0])
-def test_time_stepping_adjoint(oracles, fs):
+@pytest.mark.parametrize("fs,order", ORDERS)
+def test_time_stepping_adjoint(oracles, fs, order):
     O, _, o64 = oracles
-    cfg = small_cfg(O, fs, nt=121)
+    cfg = small_cfg(O, fs, nt=121, order=order)
     rng = np.random.default_rng(21 + fs)
     vel = rng.uniform(1500, 3000, (cfg.nz, cfg.nx)).astype(np.float32)
     sh = geometry(O, fs, rng.standard_normal(cfg.nt).astype(np.float32))
@@ -60,10 +66,10 @@ def test_time_stepping_adjoint(oracles, fs):
     assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
 
 
-@pytest.mark.parametrize("fs", [1, 0])
-def test_gradient_finite_differences(oracles, fs):
+@pytest.mark.parametrize("fs,order", ORDERS)
+def test_gradient_finite_differences(oracles, fs, order):
     O, o32, o64 = oracles
-    cfg = small_cfg(O, fs)
+    cfg = small_cfg(O, fs, order=order)
     rng = np.random.default_rng(31 + fs)
     vel = rng.uniform(1500, 3000, (cfg.nz, cfg.nx)).astype(np.float32)
     vtrue = vel.copy()
@@ -104,3 +110,37 @@ def test_multi_shot_gradient_is_sum(oracles):
     parts = [o64.gradient(cfg, vel, [s], [o]) for s, o in zip(shots, obs)]
     assert abs(J - sum(p[0] for p in parts)) <= 1e-12 * J
     assert np.allclose(g, parts[0][1] + parts[1][1], rtol=1e-12, atol=1e-30 + 1e-12 * np.abs(g).max())
+
+
+@pytest.mark.parametrize("fs,order", ORDERS)
+def test_rebuild_reproduces_forward(oracles, fs, order):
+    """The strip-based rebuild (interior operator + 2M-1 strips) retraces the
+    forward field: the interior operator equals the padded one there."""
+    O, _, o64 = oracles
+    cfg = small_cfg(O, fs, nt=161, order=order)
+    rng = np.random.default_rng(51 + fs + order)
+    vel = rng.uniform(1500, 3000, (cfg.nz, cfg.nx)).astype(np.float32)
+    sh = geometry(O, fs, ricker(cfg.nt, cfg.dt, 15.0))
+    steps = [150, 90, 40, 5]
+    fwd, reb = o64.probe(cfg, vel, sh, steps)
+    _, _, x0, z0 = o64.grid(cfg)
+    for k in range(len(steps)):
+        f = fwd[k][z0:z0 + cfg.nz, x0:x0 + cfg.nx]
+        assert np.abs(reb[k] - f).max() <= 1e-9 * np.abs(f).max(), (order, steps[k])
+
+
+def test_eighth_order_is_more_accurate(oracles):
+    """On a smooth field the 8th-order interior operator's error against the
+    analytic Laplacian is far below the 4th-order pair's."""
+    O, _, o64 = oracles
+    errs = {}
+    for order in (4, 8):
+        cfg = small_cfg(O, 1, order=order)
+        z, x = np.mgrid[0:cfg.nz, 0:cfg.nx] * 10.0
+        k = 2 * np.pi / 120.0
+        p = np.sin(k * x) * np.cos(0.7 * k * z)
+        ux, vz = o64.apply_int(cfg, p)
+        lap = -(k ** 2 + (0.7 * k) ** 2) * p
+        c = (slice(8, cfg.nz - 8), slice(8, cfg.nx - 8))
+        errs[order] = np.abs((ux + vz)[c] - lap[c]).max() / np.abs(lap[c]).max()
+    assert errs[8] < 0.05 * errs[4], errs
