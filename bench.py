@@ -69,7 +69,7 @@ def parse():
     ap.add_argument("--snap-precision", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--hbm-budget-mb", type=int, default=0, help="budget of --store auto (0: 90%% of free memory)")
     ap.add_argument("--fd-order", type=int, default=4, choices=[4, 8], help="4: the reference's; 8: the extension")
-    ap.add_argument("--skip", default="", help="comma list of: e2e,plain,cpu,strips")
+    ap.add_argument("--skip", default="", help="comma list of: e2e,plain,cpu,strips,tune")
     return ap.parse_args()
 
 
@@ -312,6 +312,11 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     eng.set_stream(stream.cuda_stream)
     eng.set_shots(shots)
+    tune = None
+    if "tune" not in skip:
+        # launch autotuner (tuning.py): a few timed steps per candidate, cached by grid and batch shape
+        import tuning
+        tune = tuning.autotune(eng, shots, vstart, cache=tuning.DEFAULT_CACHE if rank == 0 else None)
     eng.set_model(vtrue)
     obs = eng.forward()                      # observed traces from the true model (setup, untimed)
     eng.set_observed(obs)
@@ -382,7 +387,11 @@ def run_ours(args):
             "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": describe(args, cfgkw, shots, eng.stats()),
-            "gcell_steps_per_s": gcell, "gpu_launches": launches, "clocks": clocks, "roofline": roof}
+            "gcell_steps_per_s": gcell,
+            "tuning": None if tune is None else {
+                "chosen": tune["tuning"], "ms_step": tune["ms_step"], "default_ms_step": tune["default_ms_step"],
+                "trials": len(tune.get("trials", [])), "cached": tune["cached"],
+                "note": "fwd + bwd ms per time step of fwi_time_steps, before the timed region"}, "gpu_launches": launches, "clocks": clocks, "roofline": roof}
 
     # end to end through the C ABI with pinned host buffers: every step uploads the
     # model and the observed traces and reads back the misfit and the (reduced) gradient

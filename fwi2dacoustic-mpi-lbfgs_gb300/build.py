@@ -2,8 +2,8 @@
 
     python fwi2dacoustic-mpi-lbfgs_gb300/build.py [--force]
 
-Compiles ``csrc/fwi_engine.cu`` (which includes ``csrc/fwi_kernels.cuh`` and
-``csrc/fwi_kernels8.cuh``) and
+Compiles, in parallel, ``csrc/fwi_engine.cu`` (which includes
+``csrc/fwi_kernels.cuh`` and ``csrc/fwi_kernels8.cuh``) and
 ``csrc/fwi_aux.cu`` (``csrc/fwi_aux.cuh``) and ``csrc/fwi_lbfgs.cu`` with
 nvcc for ``-gencode arch=compute_103a,code=sm_103a`` into
 ``libfwigpu.so`` next to this file.  The CUDA runtime is linked statically so
@@ -41,20 +41,32 @@ def stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
+    """Compiles the three translation units in parallel, then links them."""
     if not force and not stale():
         return LIB
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-           "-I", os.path.join(ROOT, "include"), "-o", tmp] + SOURCES
+    flags = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
     # FWI_NVCC_EXTRA adds diagnostics flags, e.g. -DFWI_SELF_CHECK
-    cmd[1:1] = os.environ.get("FWI_NVCC_EXTRA", "").split()
+    flags = os.environ.get("FWI_NVCC_EXTRA", "").split() + flags
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    r = subprocess.run(cmd, capture_output=True, text=True)
+        flags.append("-Xptxas=-v")
+    objdir = os.path.join(PKG, "_build")
+    os.makedirs(objdir, exist_ok=True)
+    objs = [os.path.join(objdir, os.path.basename(src)[:-3] + ".o") for src in SOURCES]
+    procs = [subprocess.Popen([nvcc()] + flags + ["-c", src, "-o", obj], stdout=subprocess.PIPE,
+                              stderr=subprocess.PIPE, text=True) for src, obj in zip(SOURCES, objs)]
+    errors = ""
+    for p in procs:
+        out, err = p.communicate()
+        if verbose:
+            sys.stderr.write(err)
+        if p.returncode != 0:
+            errors += out + err
+    if errors:
+        raise RuntimeError("nvcc failed:\n" + errors)
+    r = subprocess.run([nvcc(), ARCH, "-shared", "-o", tmp] + objs, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + r.stdout + r.stderr)
-    if verbose:
-        sys.stderr.write(r.stderr)
+        raise RuntimeError("nvcc link failed:\n" + r.stdout + r.stderr)
     os.replace(tmp, LIB)
     return LIB
 

@@ -152,6 +152,7 @@ struct fwi_ctx {
     float* snapPsi = nullptr;      // [nsnap][nshots][pl.stride]
     unsigned* snapAmax = nullptr;  // [nsnap][nshots][2] absmax bits (F16 / BF16)
     long long store_bytes = 0;
+    fwi_tuning tune{};             // launch tuning in use, every field resolved (fwi_set_tuning)
     // FD order: M = 2 (the reference's 4th order) or M = 4 (8th order, fwi_kernels8.cuh)
     int M = 2, S = 3;              // half order, strip width 2M-1
     float* X8 = nullptr;           // M = 4: u, v (or their adjoints), rebuild u, v: 4 x nshots x fstride
@@ -297,28 +298,38 @@ RecParams rec_params(const fwi_ctx* x, float* field, int step)
     return Q;
 }
 
-// Stream of general-tile class cls.  Self-checking builds keep every launch
-// on st so that DIAG_SYNC sees each kernel finish.
+// The general-tile classes and the receiver sampling run on side streams,
+// concurrently with the interior tiles, unless the tuning says serial.
+// Self-checking builds keep every launch on st so that DIAG_SYNC sees each
+// kernel finish.
+bool concurrent(const fwi_ctx* x)
+{
 #ifdef FWI_SELF_CHECK
-constexpr bool kConcurrentClasses = false;
+    (void)x;
+    return false;
 #else
-constexpr bool kConcurrentClasses = true;
+    return x->tune.serial == 2;
 #endif
+}
 
-cudaStream_t class_stream(const fwi_ctx* x, int cls) { return kConcurrentClasses ? x->side[cls] : x->st; }
+cudaStream_t class_stream(const fwi_ctx* x, int cls) { return concurrent(x) ? x->side[cls] : x->st; }
 // Receiver sampling of step it reads p^{it+1}, which step it+2 overwrites
 // first: it runs on its own stream after step it, and step it+2 waits for it.
-constexpr bool kSampleAside = kConcurrentClasses;
+bool sample_aside(const fwi_ctx* x) { return concurrent(x); }
 
 // Launch order of the general classes (0 = x-general, 1 = z-general, 2 =
-// corners): the z-general blocks are the most and run longest, so they start
-// first (2.5% shorter forward steps than x, z, corners on C2).
-constexpr int kClassOrder[3] = {1, 0, 2};
+// corners).  By default the z-general blocks, the most numerous and longest,
+// start first (2.5% shorter forward steps than x, z, corners on C2).
+const int* class_order(const fwi_ctx* x)
+{
+    static const int z_first[3] = {1, 0, 2}, x_first[3] = {0, 1, 2};
+    return x->tune.class_order == 2 ? x_first : z_first;
+}
 
 // Forks the side streams of the non-empty classes from st.
 void fork_classes(fwi_ctx* x)
 {
-    if (!kConcurrentClasses) return;
+    if (!concurrent(x)) return;
     cudaEventRecord(x->fork_ev, x->st);
     for (int cls = 0; cls < 3; ++cls)
         if (x->gen_off[cls + 1] > x->gen_off[cls]) cudaStreamWaitEvent(x->side[cls], x->fork_ev, 0);
@@ -327,12 +338,40 @@ void fork_classes(fwi_ctx* x)
 // Joins them back: st waits for every class launched since the fork.
 void join_classes(fwi_ctx* x)
 {
-    if (!kConcurrentClasses) return;
+    if (!concurrent(x)) return;
     for (int cls = 0; cls < 3; ++cls)
         if (x->gen_off[cls + 1] > x->gen_off[cls]) {
             cudaEventRecord(x->join_ev[cls], x->side[cls]);
             cudaStreamWaitEvent(x->st, x->join_ev[cls], 0);
         }
+}
+
+// The general-tile class cls (0 = x-general, 1 = z-general, 2 = corners) in
+// the variant compiled for MB resident blocks per SM.  z-only tiles never
+// touch srx, the last member of BwdSmem.
+template <int MB>
+void launch_fwd_gen(int cls, dim3 grid, dim3 block, cudaStream_t cs, const StepParams& P)
+{
+    if (cls == 0) FWI_LAUNCH((k_fwd_gen<true, false, MB>), grid, block, 0, cs, P);
+    if (cls == 1) FWI_LAUNCH((k_fwd_gen<false, true, MB>), grid, block, 0, cs, P);
+    if (cls == 2) FWI_LAUNCH((k_fwd_gen<true, true, MB>), grid, block, 0, cs, P);
+}
+template <int MB>
+void launch_bwd_edge(int cls, dim3 grid, dim3 block, cudaStream_t cs, const StepParams& P)
+{
+    if (cls == 0) FWI_LAUNCH((k_bwd_edge<true, false, MB>), grid, block, sizeof(BwdSmem), cs, P);
+    if (cls == 1) FWI_LAUNCH((k_bwd_edge<false, true, MB>), grid, block, offsetof(BwdSmem, srx), cs, P);
+    if (cls == 2) FWI_LAUNCH((k_bwd_edge<true, true, MB>), grid, block, sizeof(BwdSmem), cs, P);
+}
+// Dynamic shared memory limits of the backward variants.
+template <int MB>
+cudaError_t set_bwd_smem()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_bwd_int<MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BWD_INT_SMEM);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bwd_edge<true, false, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BwdSmem));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bwd_edge<false, true, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BwdSmem));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bwd_edge<true, true, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BwdSmem));
+    return e;
 }
 
 // 8th-order steps (fwi_kernels8.cuh): passes over the padded grid of the n
@@ -396,21 +435,23 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi, bool sample
     } else {
     fork_classes(x);
     const int2* gen = P.gen_tiles;
-    for (const int cls : kClassOrder) {
+    for (int k = 0; k < 3; ++k) {
+        const int cls = class_order(x)[k];
         const int cnt = x->gen_off[cls + 1] - x->gen_off[cls];
         if (!cnt) continue;
         P.gen_tiles = x->gen_d + x->gen_off[cls];
         const dim3 grid(cnt, 1, n);
         cudaStream_t cs = class_stream(x, cls);
-        if (cls == 0) FWI_LAUNCH((k_fwd_gen<true, false>), grid, block, 0, cs, P);
-        if (cls == 1) FWI_LAUNCH((k_fwd_gen<false, true>), grid, block, 0, cs, P);
-        if (cls == 2) FWI_LAUNCH((k_fwd_gen<true, true>), grid, block, 0, cs, P);
+        if (x->tune.fwd_gen_blocks == 3) launch_fwd_gen<3>(cls, grid, block, cs, P);
+        else launch_fwd_gen<4>(cls, grid, block, cs, P);
         DIAG_SYNC("k_fwd_gen");
         ++l;
     }
     P.gen_tiles = gen;
     if (x->ftx1 > x->ftx0 && x->ftz1 > x->ftz0) {
-        FWI_LAUNCH(k_fwd_fast, dim3(x->ftx1 - x->ftx0, x->ftz1 - x->ftz0, n), block, 0, x->st, P);
+        const dim3 grid(x->ftx1 - x->ftx0, x->ftz1 - x->ftz0, n);
+        if (x->tune.fwd_int_blocks == 4) FWI_LAUNCH(k_fwd_fast<4>, grid, block, 0, x->st, P);
+        else FWI_LAUNCH(k_fwd_fast<6>, grid, block, 0, x->st, P);
         DIAG_SYNC("k_fwd_fast");
         ++l;
     }
@@ -422,14 +463,14 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi, bool sample
         Q.hi = x->samp_off[hi];
         if (Q.hi > Q.lo) {
             cudaStream_t ss = x->st;
-            if (kSampleAside) {
+            if (sample_aside(x)) {
                 cudaEventRecord(x->step_ev, x->st);
                 cudaStreamWaitEvent(x->samp_st, x->step_ev, 0);
                 ss = x->samp_st;
             }
             FWI_LAUNCH(k_sample, (Q.hi - Q.lo + 255) / 256, 256, 0, ss, Q);
             DIAG_SYNC("k_sample");
-            if (kSampleAside) {
+            if (sample_aside(x)) {
                 cudaEventRecord(x->samp_ev[P.step & 1], x->samp_st);
                 x->samp_pending[P.step & 1] = true;
                 x->samp_used = true;
@@ -452,21 +493,23 @@ long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
     fork_classes(x);
     // z-only tiles never touch srx (the last member of BwdSmem)
     const int2* gen = P.gen_tiles;
-    for (const int cls : kClassOrder) {
+    for (int k = 0; k < 3; ++k) {
+        const int cls = class_order(x)[k];
         const int cnt = x->gen_off[cls + 1] - x->gen_off[cls];
         if (!cnt) continue;
         P.gen_tiles = x->gen_d + x->gen_off[cls];
         const dim3 grid(cnt, 1, n);
         cudaStream_t cs = class_stream(x, cls);
-        if (cls == 0) FWI_LAUNCH((k_bwd_edge<true, false>), grid, block, sizeof(BwdSmem), cs, P);
-        if (cls == 1) FWI_LAUNCH((k_bwd_edge<false, true>), grid, block, offsetof(BwdSmem, srx), cs, P);
-        if (cls == 2) FWI_LAUNCH((k_bwd_edge<true, true>), grid, block, sizeof(BwdSmem), cs, P);
+        if (x->tune.bwd_gen_blocks == 3) launch_bwd_edge<3>(cls, grid, block, cs, P);
+        else launch_bwd_edge<4>(cls, grid, block, cs, P);
         DIAG_SYNC("k_bwd_edge");
         ++l;
     }
     P.gen_tiles = gen;
     if (x->ftx1 > x->ftx0 && x->ftz1 > x->ftz0) {
-        FWI_LAUNCH(k_bwd_int, dim3(x->ftx1 - x->ftx0, x->ftz1 - x->ftz0, n), block, BWD_INT_SMEM, x->st, P);
+        const dim3 grid(x->ftx1 - x->ftx0, x->ftz1 - x->ftz0, n);
+        if (x->tune.bwd_int_blocks == 3) FWI_LAUNCH(k_bwd_int<3>, grid, block, BWD_INT_SMEM, x->st, P);
+        else FWI_LAUNCH(k_bwd_int<4>, grid, block, BWD_INT_SMEM, x->st, P);
         DIAG_SYNC("k_bwd_int");
         ++l;
     }
@@ -911,6 +954,102 @@ int choose_store(fwi_ctx* x, int nshots, int nt_run, long long base_b, long long
     return FWI_OK;
 }
 
+// Defaults of fwi_tuning: the interior tile rectangle starts at the first
+// column (row) whose stencils reach no edge, CPML or strip cell.
+fwi_tuning default_tuning(const fwi_ctx* x)
+{
+    fwi_tuning t{};
+    const int np = x->cfg.npml;
+    t.x_first = (int)round_up(std::max(8, np + 5), 4);
+    t.z_first = x->cfg.free_surface ? 8 : (int)round_up(std::max(8, np + 5), R);
+    t.fwd_gen_blocks = 4;
+    t.bwd_gen_blocks = 4;
+    t.fwd_int_blocks = 6;
+    t.bwd_int_blocks = 4;
+    t.class_order = 1;
+    t.serial = 2;
+    return t;
+}
+
+// Tile grid and field layout of the padded grid (tuning x_first, z_first),
+// the interior tile rectangle, the general tile list, and K in that layout
+// (zero; fwi_set_model fills it).
+int set_layout(fwi_ctx* x)
+{
+    if (x->gen_d) { cudaFree(x->gen_d); x->bytes_model -= sizeof(int2) * (size_t)std::max(1, x->ngen); x->gen_d = nullptr; }
+    if (x->K) { cudaFree(x->K); x->bytes_model -= sizeof(float) * (size_t)x->g.fstride; x->K = nullptr; }
+    const fwi_config* cfg = &x->cfg;
+    Geo& g = x->g;
+    g.nx = cfg->nx; g.nz = cfg->nz; g.npml = cfg->npml; g.fs = cfg->free_surface;
+    g.pnx = cfg->nx + 2 * cfg->npml;                         // fwi_2d.c:155
+    g.pnz = cfg->nz + (g.fs ? 1 : 2) * cfg->npml;            // fwi_2d.c:155,162
+    g.x0p = cfg->npml; g.z0p = g.fs ? 0 : cfg->npml;
+    // Tile grid in x: the first interior tile starts at the first column x0i
+    // (a multiple of 4, for 16-byte staging) whose stencils reach no edge,
+    // CPML or strip cell; tile column 0 starts xoff <= 0 columns earlier.
+    // The left zero margin mx covers the halo of that first tile, and makes
+    // every tile's staged rows start on a 128-byte boundary.
+    const int x0i = x->tune.x_first;
+    g.xoff = x0i - TX * ((x0i + TX - 1) / TX);
+    const int mx = HX - g.xoff;                              // (mx + xoff - HX) == 0: aligned rows
+    g.ntx = (g.pnx - g.xoff + TX - 1) / TX;
+    // The same in z: the first interior tile starts at row z0i (a multiple
+    // of R, so the warp holding row 0 starts there, as the top formulas
+    // assume) and tile row 0 starts zoff <= 0 rows earlier, above a margin
+    // of MZ zero rows.
+    const int z0i = x->tune.z_first;
+    g.zoff = z0i - TZ * ((z0i + TZ - 1) / TZ);
+    const int mz = MZ - g.zoff;
+    g.ntz = (g.pnz - g.zoff + TZ - 1) / TZ;
+    g.ld = (int)round_up(mx + g.xoff + (long long)g.ntx * TX + HX, 32);
+    x->rows_alloc = mz + g.zoff + g.ntz * TZ + MZ;
+    g.fstride = (long long)x->rows_alloc * g.ld;
+    x->origin = (long long)mz * g.ld + mx;
+
+    // interior tile rectangle and the list of general-path tiles
+    {
+        std::vector<int2> gen;
+        int tx0 = -1, tx1 = -1, tz0 = -1, tz1 = -1;
+        for (int t = 0; t < g.ntx; ++t)
+            if (!tile_x_general(g, g.xoff + t * TX)) { if (tx0 < 0) tx0 = t; tx1 = t + 1; }
+        for (int t = 0; t < g.ntz; ++t)
+            if (!tile_z_general(g, g.zoff + t * TZ)) { if (tz0 < 0) tz0 = t; tz1 = t + 1; }
+        if (tx0 < 0 || tz0 < 0) tx0 = tx1 = tz0 = tz1 = 0;
+        // general tiles grouped by class: 0 = x-general only, 1 = z-general only, 2 = both
+        for (int cls = 0; cls < 3; ++cls) {
+            x->gen_off[cls] = (int)gen.size();
+            for (int tz = 0; tz < g.ntz; ++tz)
+                for (int tx = 0; tx < g.ntx; ++tx) {
+                    if (tx >= tx0 && tx < tx1 && tz >= tz0 && tz < tz1) continue;
+                    const bool gx = tile_x_general(g, g.xoff + tx * TX), gz = tile_z_general(g, g.zoff + tz * TZ);
+                    if (!gx && !gz) return fail(x, FWI_ERR_ARG, "tile classes do not form a rectangle");
+                    if ((gx && !gz && cls == 0) || (!gx && gz && cls == 1) || (gx && gz && cls == 2))
+                        gen.push_back(make_int2(tx, tz));
+                }
+        }
+        x->gen_off[3] = (int)gen.size();
+        x->gen_arith = 1;                                   // the kernels may compute the tiles instead
+        for (int cls = 0; cls < 3; ++cls)
+            for (int i = x->gen_off[cls]; i < x->gen_off[cls + 1]; ++i) {
+                const int2 a = gen_tile_at(g, tx0, tx1, tz0, tz1, cls != 1, cls != 0, i - x->gen_off[cls]);
+                if (a.x != gen[i].x || a.y != gen[i].y) x->gen_arith = 0;
+            }
+        x->ftx0 = tx0; x->ftx1 = tx1; x->ftz0 = tz0; x->ftz1 = tz1;
+        x->ngen = (int)gen.size();
+        if (int e = dalloc(x, &x->gen_d, gen.size(), &x->bytes_model)) return e;
+        if (!gen.empty() && cudaMemcpy(x->gen_d, gen.data(), gen.size() * sizeof(int2), cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(x, FWI_ERR_CUDA, "upload of the general tile list failed");
+    }
+
+    if (int e = dalloc(x, &x->K, (size_t)g.fstride, &x->bytes_model)) return e;
+    // on the context's stream: a legacy-stream memset would not be ordered
+    // before k_build_K, which runs on the non-blocking stream
+    if (cudaMemsetAsync(x->K, 0, sizeof(float) * g.fstride, x->st) != cudaSuccess ||
+        cudaStreamSynchronize(x->st) != cudaSuccess)
+        return fail(x, FWI_ERR_CUDA, "clearing K failed");
+    return FWI_OK;
+}
+
 // Traces longer than the XCORR kernel's shared memory holds?
 bool xcorr_too_long(const fwi_ctx* x)
 {
@@ -1021,69 +1160,11 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
         cudaEventCreateWithFlags(&x->samp_done, cudaEventDisableTiming) != cudaSuccess)
         return bail(FWI_ERR_CUDA);
 
+    x->tune = default_tuning(x);
+    if (int st = set_layout(x)) return bail(st);
+    if (dalloc(x, &x->err_d, 1, &x->bytes_model) || cudaMemset(x->err_d, 0, sizeof(int)) != cudaSuccess)
+        return bail(FWI_ERR_NOMEM);
     Geo& g = x->g;
-    g.nx = cfg->nx; g.nz = cfg->nz; g.npml = cfg->npml; g.fs = cfg->free_surface;
-    g.pnx = cfg->nx + 2 * cfg->npml;                         // fwi_2d.c:155
-    g.pnz = cfg->nz + (g.fs ? 1 : 2) * cfg->npml;            // fwi_2d.c:155,162
-    g.x0p = cfg->npml; g.z0p = g.fs ? 0 : cfg->npml;
-    // Tile grid in x: the first interior tile starts at the first column x0i
-    // (a multiple of 4, for 16-byte staging) whose stencils reach no edge,
-    // CPML or strip cell; tile column 0 starts xoff <= 0 columns earlier.
-    // The left zero margin mx covers the halo of that first tile, and makes
-    // every tile's staged rows start on a 128-byte boundary.
-    const int x0i = (int)round_up(std::max(8, g.npml + 5), 4);
-    g.xoff = x0i - TX * ((x0i + TX - 1) / TX);
-    const int mx = HX - g.xoff;                              // (mx + xoff - HX) == 0: aligned rows
-    g.ntx = (g.pnx - g.xoff + TX - 1) / TX;
-    // The same in z: the first interior tile starts at row z0i (a multiple
-    // of R, so the warp holding row 0 starts there, as the top formulas
-    // assume) and tile row 0 starts zoff <= 0 rows earlier, above a margin
-    // of MZ zero rows.
-    const int z0i = g.fs ? 8 : (int)round_up(std::max(8, g.npml + 5), R);
-    g.zoff = z0i - TZ * ((z0i + TZ - 1) / TZ);
-    const int mz = MZ - g.zoff;
-    g.ntz = (g.pnz - g.zoff + TZ - 1) / TZ;
-    g.ld = (int)round_up(mx + g.xoff + (long long)g.ntx * TX + HX, 32);
-    x->rows_alloc = mz + g.zoff + g.ntz * TZ + MZ;
-    g.fstride = (long long)x->rows_alloc * g.ld;
-    x->origin = (long long)mz * g.ld + mx;
-
-    // interior tile rectangle and the list of general-path tiles
-    {
-        std::vector<int2> gen;
-        int tx0 = -1, tx1 = -1, tz0 = -1, tz1 = -1;
-        for (int t = 0; t < g.ntx; ++t)
-            if (!tile_x_general(g, g.xoff + t * TX)) { if (tx0 < 0) tx0 = t; tx1 = t + 1; }
-        for (int t = 0; t < g.ntz; ++t)
-            if (!tile_z_general(g, g.zoff + t * TZ)) { if (tz0 < 0) tz0 = t; tz1 = t + 1; }
-        if (tx0 < 0 || tz0 < 0) tx0 = tx1 = tz0 = tz1 = 0;
-        // general tiles grouped by class: 0 = x-general only, 1 = z-general only, 2 = both
-        for (int cls = 0; cls < 3; ++cls) {
-            x->gen_off[cls] = (int)gen.size();
-            for (int tz = 0; tz < g.ntz; ++tz)
-                for (int tx = 0; tx < g.ntx; ++tx) {
-                    if (tx >= tx0 && tx < tx1 && tz >= tz0 && tz < tz1) continue;
-                    const bool gx = tile_x_general(g, g.xoff + tx * TX), gz = tile_z_general(g, g.zoff + tz * TZ);
-                    if (!gx && !gz) return bail(FWI_ERR_ARG);     // cannot happen: such tiles form the rectangle
-                    if ((gx && !gz && cls == 0) || (!gx && gz && cls == 1) || (gx && gz && cls == 2))
-                        gen.push_back(make_int2(tx, tz));
-                }
-        }
-        x->gen_off[3] = (int)gen.size();
-        x->gen_arith = 1;                                   // the kernels may compute the tiles instead
-        for (int cls = 0; cls < 3; ++cls)
-            for (int i = x->gen_off[cls]; i < x->gen_off[cls + 1]; ++i) {
-                const int2 a = gen_tile_at(g, tx0, tx1, tz0, tz1, cls != 1, cls != 0, i - x->gen_off[cls]);
-                if (a.x != gen[i].x || a.y != gen[i].y) x->gen_arith = 0;
-            }
-        x->ftx0 = tx0; x->ftx1 = tx1; x->ftz0 = tz0; x->ftz1 = tz1;
-        x->ngen = (int)gen.size();
-        if (dalloc(x, &x->gen_d, gen.size(), &x->bytes_model)) return bail(FWI_ERR_NOMEM);
-        if (dalloc(x, &x->err_d, 1, &x->bytes_model) || cudaMemset(x->err_d, 0, sizeof(int)) != cudaSuccess)
-            return bail(FWI_ERR_NOMEM);
-        if (!gen.empty() && cudaMemcpy(x->gen_d, gen.data(), gen.size() * sizeof(int2), cudaMemcpyHostToDevice) != cudaSuccess)
-            return bail(FWI_ERR_CUDA);
-    }
 
     float fd[8];
     fd_coefficients(cfg->dx, cfg->dz, fd);
@@ -1131,25 +1212,11 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
         a1z[i] = a0z[2 * np - i]; b1z[i] = b0z[2 * np - i];
     }
     if (dalloc(x, &x->pmlc, h.size(), &x->bytes_model)) return bail(FWI_ERR_NOMEM);
-    if (dalloc(x, &x->K, (size_t)g.fstride, &x->bytes_model)) return bail(FWI_ERR_NOMEM);
     if (dalloc(x, &x->vel, (size_t)g.nx * g.nz, &x->bytes_model)) return bail(FWI_ERR_NOMEM);
     if (dalloc(x, &x->grad, (size_t)g.nx * g.nz, &x->bytes_model)) return bail(FWI_ERR_NOMEM);
     if (dalloc(x, &x->gradf, (size_t)g.nx * g.nz, &x->bytes_model)) return bail(FWI_ERR_NOMEM);
     if (cudaMemcpy(x->pmlc, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return bail(FWI_ERR_CUDA);
-    // on the context's stream: a legacy-stream memset would not be ordered
-    // before k_build_K, which runs on the non-blocking stream
-    if (cudaMemsetAsync(x->K, 0, sizeof(float) * g.fstride, x->st) != cudaSuccess ||
-        cudaStreamSynchronize(x->st) != cudaSuccess)
-        return bail(FWI_ERR_CUDA);
-    if (cudaFuncSetAttribute(k_bwd_int, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BWD_INT_SMEM) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(k_bwd_edge<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(BwdSmem)) != cudaSuccess ||
-        cudaFuncSetAttribute(k_bwd_edge<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(BwdSmem)) != cudaSuccess ||
-        cudaFuncSetAttribute(k_bwd_edge<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(BwdSmem)) != cudaSuccess)
-        return bail(FWI_ERR_CUDA);
+    if (set_bwd_smem<3>() != cudaSuccess || set_bwd_smem<4>() != cudaSuccess) return bail(FWI_ERR_CUDA);
     if (status) *status = FWI_OK;
     return x;
 }
@@ -1624,6 +1691,85 @@ int fwi_set_stream(fwi_ctx* x, void* stream)
     CK(cudaSetDevice(x->cfg.device));
     CK(cudaStreamSynchronize(x->st));
     x->st = stream ? (cudaStream_t)stream : x->own;
+    return FWI_OK;
+}
+
+int fwi_set_tuning(fwi_ctx* x, const fwi_tuning* t)
+{
+    if (!x || !t) return FWI_ERR_ARG;
+    for (int i = 0; i < 8; ++i)
+        if (t->reserved[i]) return fail(x, FWI_ERR_ARG, "fwi_tuning.reserved must be zero");
+    const fwi_tuning d = default_tuning(x);
+    fwi_tuning n = x->tune;
+    auto pick = [](int v, int cur) { return v ? v : cur; };
+    n.x_first = t->x_first ? t->x_first : d.x_first;
+    n.z_first = t->z_first ? t->z_first : d.z_first;
+    n.fwd_gen_blocks = pick(t->fwd_gen_blocks, d.fwd_gen_blocks);
+    n.bwd_gen_blocks = pick(t->bwd_gen_blocks, d.bwd_gen_blocks);
+    n.fwd_int_blocks = pick(t->fwd_int_blocks, d.fwd_int_blocks);
+    n.bwd_int_blocks = pick(t->bwd_int_blocks, d.bwd_int_blocks);
+    n.class_order = pick(t->class_order, d.class_order);
+    n.serial = pick(t->serial, d.serial);
+    const Geo& g = x->g;
+    if (n.x_first < d.x_first || n.x_first % 4 || n.x_first >= g.pnx - g.npml - 4)
+        return fail(x, FWI_ERR_ARG, "x_first must be a multiple of 4 from " + std::to_string(d.x_first));
+    if (n.z_first < d.z_first || n.z_first % R || n.z_first >= g.pnz - 4)
+        return fail(x, FWI_ERR_ARG, "z_first must be a multiple of 4 from " + std::to_string(d.z_first));
+    if ((n.fwd_gen_blocks != 3 && n.fwd_gen_blocks != 4) || (n.bwd_gen_blocks != 3 && n.bwd_gen_blocks != 4) ||
+        (n.fwd_int_blocks != 4 && n.fwd_int_blocks != 6) || (n.bwd_int_blocks != 3 && n.bwd_int_blocks != 4) ||
+        (n.class_order != 1 && n.class_order != 2) || (n.serial != 1 && n.serial != 2))
+        return fail(x, FWI_ERR_ARG, "a fwi_tuning value outside its list");
+    CK(cudaSetDevice(x->cfg.device));
+    CK(cudaStreamSynchronize(x->st));
+    const bool relayout = n.x_first != x->tune.x_first || n.z_first != x->tune.z_first;
+    x->tune = n;
+    drop_graph(x);                       // the captured phases hold the old launches
+    if (relayout) {
+        free_shots(x);
+        x->have_model = false;
+        if (int st = set_layout(x)) return st;
+    }
+    return FWI_OK;
+}
+
+int fwi_get_tuning(const fwi_ctx* x, fwi_tuning* out)
+{
+    if (!x || !out) return FWI_ERR_ARG;
+    *out = x->tune;
+    return FWI_OK;
+}
+
+int fwi_time_steps(fwi_ctx* x, int steps, double* ms_fwd, double* ms_bwd)
+{
+    if (!x || steps < 1 || !ms_fwd || !ms_bwd) return FWI_ERR_ARG;
+    if (usable(x)) return FWI_ERR_STATE;
+    if (!x->have_model || !x->nshots) return fail(x, FWI_ERR_STATE, "fwi_set_model and fwi_set_shots first");
+    CK(cudaSetDevice(x->cfg.device));
+    const long long half = (long long)x->nshots * x->g.fstride;
+    const long long phalf = (long long)x->nshots * x->pl.stride;
+    // backward steps from the end of the record read the strips the ring holds
+    // for them: with checkpoints, those of the last segment
+    const int last_seg = x->nt_run - (x->nseg - 1) * x->seg;
+    const int nf = std::min(steps, x->nt_run);
+    const int nb = std::min(steps, x->store == FWI_STORE_SNAPSHOTS ? last_seg : x->nt_run);
+    x->have_fwd = false;
+    CK(cudaMemsetAsync(x->F, 0, sizeof(float) * 2 * half, x->st));
+    CK(cudaMemsetAsync(x->psiF, 0, sizeof(float) * 2 * phalf, x->st));
+    CK(cudaMemsetAsync(x->A, 0, sizeof(float) * 2 * half, x->st));
+    CK(cudaMemsetAsync(x->psiA, 0, sizeof(float) * 2 * phalf, x->st));
+    StepParams P = base_params(x);
+    P.gacc = x->Gacc + x->origin;
+    set_ring(x, P, x->nseg - 1);
+    CK(cudaEventRecord(x->ev[0], x->st));
+    forward_steps(x, P, 0, nf, 0, x->nshots, false);
+    CK(cudaEventRecord(x->ev[1], x->st));
+    backward_steps(x, P, x->nt_run, x->nt_run - nb, 0, x->nshots);
+    CK(cudaEventRecord(x->ev[2], x->st));
+    CK(cudaGetLastError());
+    int s = finish(x);
+    if (s) return s;
+    *ms_fwd = event_ms(x->ev[0], x->ev[1]) / nf;
+    *ms_bwd = event_ms(x->ev[1], x->ev[2]) / nb;
     return FWI_OK;
 }
 

@@ -706,9 +706,12 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
 }
 
 // Forward step, tiles of the general path (edges, CPML, strips) of one
-// class (GX, GZ), from the list P.gen_tiles.
-template <bool GX, bool GZ>
-__global__ void __launch_bounds__(NTH, 4) k_fwd_gen(const StepParams P)
+// class (GX, GZ), from the list P.gen_tiles.  MINB (here and on k_fwd_fast,
+// k_bwd_edge, k_bwd_int): the resident blocks per SM that the register
+// budget is sized for; the engine instantiates the variants its tuning
+// (fwi_tuning) chooses from.
+template <bool GX, bool GZ, int MINB>
+__global__ void __launch_bounds__(NTH, MINB) k_fwd_gen(const StepParams P)
 {
     __shared__ __align__(16) float sp[SPH * SPW];
     __shared__ __align__(16) float su[TZ * UWP];
@@ -730,7 +733,8 @@ __global__ void __launch_bounds__(NTH, 4) k_fwd_gen(const StepParams P)
 // takes the same branch-free stencil, its x part as dxx7 of the staged tile.
 // The per-cell loads of p^{it-1} and K are issued before the tile copy so
 // that their latencies overlap.
-__global__ void __launch_bounds__(NTH, 6) k_fwd_fast(const __grid_constant__ StepParams P)
+template <int MINB>
+__global__ void __launch_bounds__(NTH, MINB) k_fwd_fast(const __grid_constant__ StepParams P)
 {
     __shared__ __align__(128) float sp[SPH * SPW];
     __shared__ __align__(8) unsigned long long bar;
@@ -1075,8 +1079,8 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
 
 // Backward step, tiles of the general path (edges, CPML, strips) of one
 // class (GX, GZ), from the list P.gen_tiles.
-template <bool GX, bool GZ>
-__global__ void __launch_bounds__(NTH, 4) k_bwd_edge(const StepParams P)
+template <bool GX, bool GZ, int MINB>
+__global__ void __launch_bounds__(NTH, MINB) k_bwd_edge(const StepParams P)
 {
     FWI_DYN_SMEM(smraw);
     BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
@@ -1225,7 +1229,8 @@ constexpr size_t BWD_INT_SMEM = sizeof(BwdIntSmem) + 128;
 // (Copying p^m and g into shared memory instead was 5% slower: 55 KB per
 // block leaves too little of the SM's shared memory and L1 for the
 // concurrent general blocks.)
-__global__ void __launch_bounds__(NTH, 4) k_bwd_int(const __grid_constant__ StepParams P)
+template <int MINB>
+__global__ void __launch_bounds__(NTH, MINB) k_bwd_int(const __grid_constant__ StepParams P)
 {
     FWI_DYN_SMEM(smraw);
 #ifdef FWI_CPU_EMU

@@ -101,6 +101,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.fwi_lbfgs_begin.argtypes = [P, C.POINTER(D), D, P, I, C.POINTER(I)]
     lib.fwi_lbfgs_next.argtypes = [P, C.POINTER(D), D, P, I, C.POINTER(I)]
     lib.fwi_lbfgs_info.argtypes = [P, C.POINTER(I), C.POINTER(D), C.POINTER(I)]
+    lib.fwi_set_tuning.argtypes = [P, C.POINTER(FwiTuning)]
+    lib.fwi_get_tuning.argtypes = [P, C.POINTER(FwiTuning)]
+    lib.fwi_time_steps.argtypes = [P, I, C.POINTER(D), C.POINTER(D)]
     _LIB = lib
     return lib
 
@@ -109,6 +112,15 @@ class FwiMisfit(C.Structure):
     """fwi_misfit (include/fwi_gb300.h)."""
     _fields_ = [("kind", C.c_int), ("slice", C.c_int), ("offset_min", C.c_float), ("offset_max", C.c_float),
                 ("reserved", C.c_int * 4)]
+
+
+class FwiTuning(C.Structure):
+    """fwi_tuning (include/fwi_gb300.h): run-time launch choices, 0 = default."""
+    _fields_ = [("x_first", C.c_int), ("z_first", C.c_int), ("fwd_gen_blocks", C.c_int), ("bwd_gen_blocks", C.c_int),
+                ("fwd_int_blocks", C.c_int), ("bwd_int_blocks", C.c_int), ("class_order", C.c_int),
+                ("serial", C.c_int), ("reserved", C.c_int * 8)]
+    KEYS = ("x_first", "z_first", "fwd_gen_blocks", "bwd_gen_blocks", "fwd_int_blocks", "bwd_int_blocks",
+            "class_order", "serial")
 
 
 class FwiLbfgsParam(C.Structure):
@@ -275,6 +287,28 @@ class Engine:
         ``torch.cuda.current_stream().cuda_stream``); None restores the own stream."""
         self._check(self.lib.fwi_set_stream(self.ctx, C.c_void_p(stream_ptr) if stream_ptr else None),
                     "fwi_set_stream")
+
+    def set_tuning(self, tuning: dict):
+        """fwi_set_tuning from a dict of FwiTuning fields (missing or 0 = default).
+        Changing x_first / z_first discards the shots and the model."""
+        t = FwiTuning()
+        for k, v in tuning.items():
+            setattr(t, k, int(v))
+        relayout = any(tuning.get(k, 0) and tuning.get(k) != self.tuning()[k] for k in ("x_first", "z_first"))
+        self._check(self.lib.fwi_set_tuning(self.ctx, C.byref(t)), "fwi_set_tuning")
+        if relayout:
+            self.shots = []
+
+    def tuning(self) -> dict:
+        t = FwiTuning()
+        self._check(self.lib.fwi_get_tuning(self.ctx, C.byref(t)), "fwi_get_tuning")
+        return {k: getattr(t, k) for k in FwiTuning.KEYS}
+
+    def time_steps(self, steps: int):
+        """(ms per forward step, ms per backward step) of the current batch."""
+        f, b = C.c_double(), C.c_double()
+        self._check(self.lib.fwi_time_steps(self.ctx, int(steps), C.byref(f), C.byref(b)), "fwi_time_steps")
+        return f.value, b.value
 
     def stats(self) -> dict:
         s = FwiStats()

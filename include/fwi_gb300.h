@@ -217,6 +217,46 @@ const double *fwi_grad_device(const fwi_ctx *ctx);
 int fwi_set_stream(fwi_ctx *ctx, void *stream);
 
 int fwi_get_stats(const fwi_ctx *ctx, fwi_stats *out);
+
+/* ---- launch tuning (no counterpart in the reference) -------------------- */
+/* What the kernels allow to be chosen at run time.  The tile is 64 x 32
+ * cells per 256 threads at compile time: the staging, the thread-to-cell
+ * mapping and the register budgets of the kernels are built around it.  A
+ * zero field keeps the default.
+ *   x_first, z_first: first padded column / row of the interior tile
+ *       rectangle (the tile grid is laid from there; default the first
+ *       column / row whose stencils reach no edge, CPML or strip cell,
+ *       round_up(max(8, npml + 5), 4), and row 8 with a free surface); a
+ *       multiple of 4 no smaller than the default.  Changing them re-lays
+ *       the fields: fwi_set_tuning then discards the shots and the model,
+ *       which must be set again.
+ *   fwd_gen_blocks, bwd_gen_blocks: resident blocks per SM the general-tile
+ *       kernels are compiled for, 3 or 4 (default 4);
+ *   fwd_int_blocks: the interior forward kernel, 4 or 6 (default 6);
+ *   bwd_int_blocks: the interior backward kernel, 3 or 4 (default 4);
+ *   class_order: 1 launches the z-general class first (default), 2 the
+ *       x-general class first;
+ *   serial: 1 runs the general classes and the receiver sampling on the
+ *       context's stream, 2 (default) on their own streams, concurrently
+ *       with the interior tiles. */
+typedef struct fwi_tuning {
+    int x_first, z_first;
+    int fwd_gen_blocks, bwd_gen_blocks;
+    int fwd_int_blocks, bwd_int_blocks;
+    int class_order;
+    int serial;
+    int reserved[8];       /* zero */
+} fwi_tuning;
+/* FWI_ERR_ARG for a value outside the lists above. */
+int fwi_set_tuning(fwi_ctx *ctx, const fwi_tuning *tuning);
+/* The tuning in use, every field resolved (no zeros). */
+int fwi_get_tuning(const fwi_ctx *ctx, fwi_tuning *out);
+/* Times `steps` forward and `steps` backward time steps of the current shot
+ * batch (after fwi_set_shots and fwi_set_model) and returns the average
+ * device time of one step of each; the fields they compute are discarded
+ * (a following fwi_backward needs a new fwi_forward).  For sweeps over
+ * fwi_tuning; the 8th-order path has nothing to tune but the serial flag. */
+int fwi_time_steps(fwi_ctx *ctx, int steps, double *ms_forward_step, double *ms_backward_step);
 const char *fwi_status_string(int status);
 const char *fwi_last_error(const fwi_ctx *ctx);   /* detail of the last failure */
 int fwi_version(void);

@@ -1,7 +1,8 @@
 """One gradient through the CPU emulation build of the engine, checked
 against the FP64 oracle; run by test_emu_sanitized.py in a child process
 with AddressSanitizer and UBSan preloaded and FWI_LIB pointing at
-libfwiemu.so.  Arguments: free surface, nt, nx, nz [, nseg [, fd_order]].
+libfwiemu.so.  Arguments: free surface, nt, nx, nz [, nseg [, fd_order [,
+x shift, z shift of the tile grid (fwi_tuning)]]].
 Prints one JSON line {J, J64, grad_rel, syn_rel}.  With nseg > 0 the same gradient is also taken with checkpoints
 (FWI_STORE_SNAPSHOTS, nseg segments) in FP32 and FP16 storage (BF16 shares
 the FP16 path but for its rounding) and the line adds {snap_f32_rel,
@@ -21,12 +22,17 @@ import oracle as O                         # noqa: E402
 from test_gpu_parity import Case, rel      # noqa: E402
 
 
-def main(fs, nt, nx=150, nz=90, nseg=0, order=4):
+def main(fs, nt, nx=150, nz=90, nseg=0, order=4, xshift=0, zshift=0):
     o64 = O.Oracle("f64")
     case = Case(O, fs, seed=11 + fs, nt=nt, nx=nx, nz=nz, order=order)
     case.vtrue = (case.vel * 1.08).astype(np.float32)    # signal in the direct waves of a short record
     obs = case.oracle_obs(o64)
     e = case.engine()
+    if xshift or zshift:                 # another tile grid (fwi_tuning x_first / z_first)
+        t = e.tuning()
+        e.set_tuning({"x_first": t["x_first"] + xshift, "z_first": t["z_first"] + zshift,
+                      "fwd_gen_blocks": 3, "bwd_int_blocks": 3, "class_order": 2, "serial": 1})
+        e.set_shots(case.eshots)
     e.set_model(case.vel)
     syn = e.split(e.forward())
     syn_rel = max(rel(got, o64.forward(case.oracle_cfg_for(len(s.wav)), case.vel, s))

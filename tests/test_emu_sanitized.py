@@ -46,12 +46,16 @@ def emu_lib():
 # (free surface, nx, nz): 150 x 90 has full-width edge tiles; 130 x 70 leaves a
 # last tile column under half a tile wide and a last tile row of a few rows,
 # which exercises the skipped padding halves and rows.
-@pytest.mark.parametrize("fs,nx,nz", [(1, 150, 90), (0, 150, 90), (1, 130, 70), (0, 130, 70)])
-def test_emulated_gradient_is_memory_safe_and_matches_oracle(emu_lib, oracles, fs, nx, nz):
+# The last two cases also lay the tile grid elsewhere (fwi_tuning x_first /
+# z_first shifted) with the other kernel variants, class order and serial launches.
+@pytest.mark.parametrize("fs,nx,nz,xs,zs", [(1, 150, 90, 0, 0), (0, 130, 70, 0, 0), (1, 130, 70, 8, 4),
+                                           (0, 150, 90, 32, 16)])
+def test_emulated_gradient_is_memory_safe_and_matches_oracle(emu_lib, oracles, fs, nx, nz, xs, zs):
     lib, libs = emu_lib
     env = dict(os.environ, FWI_LIB=lib, LD_PRELOAD=" ".join(libs),
                ASAN_OPTIONS="detect_leaks=0:abort_on_error=1", UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1")
-    r = subprocess.run([sys.executable, os.path.join(HERE, "emu_gradient_case.py"), str(fs), "41", str(nx), str(nz)],
+    r = subprocess.run([sys.executable, os.path.join(HERE, "emu_gradient_case.py"), str(fs), "41", str(nx), str(nz),
+                        "0", "4", str(xs), str(zs)],
                        capture_output=True, text=True, env=env, timeout=900)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-6000:]
     assert "ERROR: AddressSanitizer" not in r.stderr and "runtime error" not in r.stderr, r.stderr[-6000:]
