@@ -968,7 +968,23 @@ fwi_tuning default_tuning(const fwi_ctx* x)
     t.bwd_int_blocks = 4;
     t.class_order = 1;
     t.serial = 2;
+    t.priority = 1;
     return t;
+}
+
+// (Re)creates the general classes' side streams at the tuning's priority.
+cudaError_t make_side_streams(fwi_ctx* x)
+{
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e != cudaSuccess) return e;
+    for (int i = 0; i < 3; ++i) {
+        if (x->side[i]) cudaStreamDestroy(x->side[i]);
+        x->side[i] = nullptr;
+        e = cudaStreamCreateWithPriority(&x->side[i], cudaStreamNonBlocking, x->tune.priority == 2 ? greatest : 0);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 // Tile grid and field layout of the padded grid (tuning x_first, z_first),
@@ -1148,10 +1164,10 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     x->st = x->own;
     for (auto& e : x->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return bail(FWI_ERR_CUDA);
+    x->tune = default_tuning(x);
+    if (make_side_streams(x) != cudaSuccess) return bail(FWI_ERR_CUDA);
     for (int i = 0; i < 3; ++i)
-        if (cudaStreamCreateWithFlags(&x->side[i], cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&x->join_ev[i], cudaEventDisableTiming) != cudaSuccess)
-            return bail(FWI_ERR_CUDA);
+        if (cudaEventCreateWithFlags(&x->join_ev[i], cudaEventDisableTiming) != cudaSuccess) return bail(FWI_ERR_CUDA);
     if (cudaEventCreateWithFlags(&x->fork_ev, cudaEventDisableTiming) != cudaSuccess) return bail(FWI_ERR_CUDA);
     if (cudaStreamCreateWithFlags(&x->samp_st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&x->step_ev, cudaEventDisableTiming) != cudaSuccess ||
@@ -1160,7 +1176,6 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
         cudaEventCreateWithFlags(&x->samp_done, cudaEventDisableTiming) != cudaSuccess)
         return bail(FWI_ERR_CUDA);
 
-    x->tune = default_tuning(x);
     if (int st = set_layout(x)) return bail(st);
     if (dalloc(x, &x->err_d, 1, &x->bytes_model) || cudaMemset(x->err_d, 0, sizeof(int)) != cudaSuccess)
         return bail(FWI_ERR_NOMEM);
@@ -1697,7 +1712,7 @@ int fwi_set_stream(fwi_ctx* x, void* stream)
 int fwi_set_tuning(fwi_ctx* x, const fwi_tuning* t)
 {
     if (!x || !t) return FWI_ERR_ARG;
-    for (int i = 0; i < 8; ++i)
+    for (int i = 0; i < 7; ++i)
         if (t->reserved[i]) return fail(x, FWI_ERR_ARG, "fwi_tuning.reserved must be zero");
     const fwi_tuning d = default_tuning(x);
     fwi_tuning n = x->tune;
@@ -1710,6 +1725,7 @@ int fwi_set_tuning(fwi_ctx* x, const fwi_tuning* t)
     n.bwd_int_blocks = pick(t->bwd_int_blocks, d.bwd_int_blocks);
     n.class_order = pick(t->class_order, d.class_order);
     n.serial = pick(t->serial, d.serial);
+    n.priority = pick(t->priority, d.priority);
     const Geo& g = x->g;
     if (n.x_first < d.x_first || n.x_first % 4 || n.x_first >= g.pnx - g.npml - 4)
         return fail(x, FWI_ERR_ARG, "x_first must be a multiple of 4 from " + std::to_string(d.x_first));
@@ -1717,13 +1733,16 @@ int fwi_set_tuning(fwi_ctx* x, const fwi_tuning* t)
         return fail(x, FWI_ERR_ARG, "z_first must be a multiple of 4 from " + std::to_string(d.z_first));
     if ((n.fwd_gen_blocks != 3 && n.fwd_gen_blocks != 4) || (n.bwd_gen_blocks != 3 && n.bwd_gen_blocks != 4) ||
         (n.fwd_int_blocks != 4 && n.fwd_int_blocks != 6) || (n.bwd_int_blocks != 3 && n.bwd_int_blocks != 4) ||
-        (n.class_order != 1 && n.class_order != 2) || (n.serial != 1 && n.serial != 2))
+        (n.class_order != 1 && n.class_order != 2) || (n.serial != 1 && n.serial != 2) ||
+        (n.priority != 1 && n.priority != 2))
         return fail(x, FWI_ERR_ARG, "a fwi_tuning value outside its list");
     CK(cudaSetDevice(x->cfg.device));
     CK(cudaStreamSynchronize(x->st));
     const bool relayout = n.x_first != x->tune.x_first || n.z_first != x->tune.z_first;
+    const bool reprio = n.priority != x->tune.priority;
     x->tune = n;
     drop_graph(x);                       // the captured phases hold the old launches
+    if (reprio) CK(make_side_streams(x));
     if (relayout) {
         free_shots(x);
         x->have_model = false;

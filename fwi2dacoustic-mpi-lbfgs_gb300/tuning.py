@@ -11,8 +11,9 @@ chosen at run time (include/fwi_gb300.h, ``fwi_tuning``):
 * the occupancy each heavy kernel's register budget is compiled for
   (``fwd_gen_blocks``, ``bwd_gen_blocks``, ``fwd_int_blocks``,
   ``bwd_int_blocks``);
-* the launch order of the general classes and whether they run concurrently
-  with the interior tiles (``class_order``, ``serial``).
+* the launch order of the general classes, whether they run concurrently
+  with the interior tiles and at which stream priority (``class_order``,
+  ``serial``, ``priority``).
 
 ``autotune`` times a few forward and backward steps of the actual shot batch
 (``fwi_time_steps``) for each candidate, first the tile grid (coordinate by
@@ -29,7 +30,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_CACHE = os.path.join(PKG, "tuning_cache.json")
 
 KNOBS = (("fwd_gen_blocks", (4, 3)), ("bwd_gen_blocks", (4, 3)), ("fwd_int_blocks", (6, 4)),
-         ("bwd_int_blocks", (4, 3)), ("class_order", (1, 2)), ("serial", (2, 1)))
+         ("bwd_int_blocks", (4, 3)), ("class_order", (1, 2)), ("serial", (2, 1)), ("priority", (1, 2)))
 
 
 def cache_key(cfg, shots) -> str:
@@ -104,7 +105,7 @@ def autotune(eng, shots, vel, steps: int = 12, cache: str | None = DEFAULT_CACHE
         for shift in (4, 8, 16):
             trial(dict(best_t, z_first=base["z_first"] + shift))
     for knob, values in KNOBS:
-        if eighth and knob != "serial":
+        if eighth and knob not in ("serial", "priority"):
             continue                                # the 8th-order passes have one variant each
         for v in values:
             if v != best_t[knob]:

@@ -238,14 +238,18 @@ int fwi_get_stats(const fwi_ctx *ctx, fwi_stats *out);
  *       x-general class first;
  *   serial: 1 runs the general classes and the receiver sampling on the
  *       context's stream, 2 (default) on their own streams, concurrently
- *       with the interior tiles. */
+ *       with the interior tiles;
+ *   priority: 1 (default) gives the general classes' streams the same
+ *       priority as the context's stream, 2 the device's highest, so that
+ *       their (longer) blocks are scheduled first as SMs free up. */
 typedef struct fwi_tuning {
     int x_first, z_first;
     int fwd_gen_blocks, bwd_gen_blocks;
     int fwd_int_blocks, bwd_int_blocks;
     int class_order;
     int serial;
-    int reserved[8];       /* zero */
+    int priority;
+    int reserved[7];       /* zero */
 } fwi_tuning;
 /* FWI_ERR_ARG for a value outside the lists above. */
 int fwi_set_tuning(fwi_ctx *ctx, const fwi_tuning *tuning);
