@@ -256,7 +256,17 @@ __global__ void __launch_bounds__(256) k8_adj_uv(const StepParams P, Step8 B)
     const float* y = P.bcur + so;
     const float* psr = P.psr + (long long)s * P.pl.stride;
     float* psw = P.psw + (long long)s * P.pl.stride;
-    if (r < g.pnz) {
+    const int np = g.npml;
+    // Away from the edges and the CPML every cell the gathers read is an
+    // 8th-order cell without psi: ubar(j) = sum_k w_k (y[j-k] - y[j+k-1]), the
+    // same weights as w8m, without evaluating them term by term.
+    const bool fast_x = j - 4 >= max(np, 3) && j + 3 <= min(g.pnx - np - 1, g.pnx - 4);
+    const bool fast_z = r - 4 >= 3 && r + 3 <= g.pnz - 4 && r + 3 < g.pnz - np - 1 && (g.fs || r - 4 > np);
+    if (r < g.pnz && fast_x) {
+        const float* a = y + (long long)r * g.ld;
+        B.U[so + (long long)r * g.ld + j] = cf.w8x[0] * (a[j - 1] - a[j]) + cf.w8x[1] * (a[j - 2] - a[j + 1]) +
+                                            cf.w8x[2] * (a[j - 3] - a[j + 2]) + cf.w8x[3] * (a[j - 4] - a[j + 3]);
+    } else if (r < g.pnz) {
         float acc = 0.f;
         for (int i = j - 4; i <= j + 3; ++i) {
             const float wgt = w8m(i, j, g.pnx, cf.w8x, cf.c0x, cf.c1x, cf.ix, 0.f, false);
@@ -268,7 +278,13 @@ __global__ void __launch_bounds__(256) k8_adj_uv(const StepParams P, Step8 B)
             psi_adj(psi_ux(P, r, j), psr, psw, a0x, b0x, a1x, b1x, y[(long long)r * g.ld + j], true);
         B.U[so + (long long)r * g.ld + j] = psi_adj(psi_u(P, r, j), psr, psw, a0x, b0x, a1x, b1x, acc, true);
     }
-    if (j < g.pnx) {
+    if (j < g.pnx && fast_z) {
+        const float* a = y + j;
+        const long long L = g.ld;
+        B.V[so + (long long)r * g.ld + j] =
+            cf.w8z[0] * (a[(r - 1) * L] - a[r * L]) + cf.w8z[1] * (a[(r - 2) * L] - a[(r + 1) * L]) +
+            cf.w8z[2] * (a[(r - 3) * L] - a[(r + 2) * L]) + cf.w8z[3] * (a[(r - 4) * L] - a[(r + 3) * L]);
+    } else if (j < g.pnx) {
         float acc = 0.f;
         for (int k = r - 4; k <= r + 3; ++k) {
             const float wgt = w8m(k, r, g.pnz, cf.w8z, cf.c0z, cf.c1z, cf.iz, cf.iz24, g.fs != 0);
@@ -310,13 +326,28 @@ __global__ void __launch_bounds__(256) k8_adj(const StepParams P, Step8 B)
     if (P.step > P.shots[s].nt) return;
     const long long so = (long long)s * g.fstride, o = so + (long long)r * g.ld + c;
     float pbar = 0.f;
-    for (int j = c - 3; j <= c + 4; ++j) {
-        const float wgt = w8p(j, c, g.pnx, cf.w8x, cf.c0x, cf.c1x, cf.ix, 0.f, false);
-        if (wgt != 0.f) pbar = fmaf(wgt, B.U[so + (long long)r * g.ld + j], pbar);
+    // where every position read is an 8th-order one (c in [7, pnx-8]):
+    // sum_k w_k (ubar[c-k+1] - ubar[c+k]), the weights of w8p
+    if (c >= 7 && c <= g.pnx - 8) {
+        const float* u = B.U + so + (long long)r * g.ld;
+        pbar = cf.w8x[0] * (u[c] - u[c + 1]) + cf.w8x[1] * (u[c - 1] - u[c + 2]) + cf.w8x[2] * (u[c - 2] - u[c + 3]) +
+               cf.w8x[3] * (u[c - 3] - u[c + 4]);
+    } else {
+        for (int j = c - 3; j <= c + 4; ++j) {
+            const float wgt = w8p(j, c, g.pnx, cf.w8x, cf.c0x, cf.c1x, cf.ix, 0.f, false);
+            if (wgt != 0.f) pbar = fmaf(wgt, B.U[so + (long long)r * g.ld + j], pbar);
+        }
     }
-    for (int kv = r - 3; kv <= r + 4; ++kv) {
-        const float wgt = w8p(kv, r, g.pnz, cf.w8z, cf.c0z, cf.c1z, cf.iz, cf.iz840, g.fs != 0);
-        if (wgt != 0.f) pbar = fmaf(wgt, B.V[so + (long long)kv * g.ld + c], pbar);
+    if (r >= 7 && r <= g.pnz - 8) {
+        const float* v = B.V + so + c;
+        const long long L = g.ld;
+        pbar += cf.w8z[0] * (v[r * L] - v[(r + 1) * L]) + cf.w8z[1] * (v[(r - 1) * L] - v[(r + 2) * L]) +
+                cf.w8z[2] * (v[(r - 2) * L] - v[(r + 3) * L]) + cf.w8z[3] * (v[(r - 3) * L] - v[(r + 4) * L]);
+    } else {
+        for (int kv = r - 3; kv <= r + 4; ++kv) {
+            const float wgt = w8p(kv, r, g.pnz, cf.w8z, cf.c0z, cf.c1z, cf.iz, cf.iz840, g.fs != 0);
+            if (wgt != 0.f) pbar = fmaf(wgt, B.V[so + (long long)kv * g.ld + c], pbar);
+        }
     }
     const float kk = P.K[(long long)r * g.ld + c];
     P.bold[o] = fmaf(kk, pbar, fmaf(2.f, P.bcur[o], -P.bold[o]));
