@@ -4,7 +4,9 @@
 // optimizer takes one line-search decision per evaluation.  All vectors
 // (x, the saved xp / gp, the direction d and the m correction pairs s, y)
 // live in HBM in FP64; dot products are deterministic two-pass FP64
-// reductions.  The decisions, step rules and two-loop recursion are those
+// reductions.  The host waits only for the values the line search decides
+// on (the slopes g.d, |x| and |g|) and for the trial point it hands out; the
+// two-loop recursion keeps its coefficients on the device.  The decisions, step rules and two-loop recursion are those
 // of MBotOpt.c (see fwi_gb300.h).
 #include "fwi_gb300.h"
 #ifdef FWI_CPU_EMU
@@ -52,13 +54,6 @@ __global__ void k_dot_final(const double* __restrict__ part, int n, double* __re
     }
 }
 
-// y = a * x + b * y
-__global__ void k_axpby(double* __restrict__ y, const double* __restrict__ x, double a, double b, long long n)
-{
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        y[i] = a * x[i] + b * y[i];
-}
-
 // y = -x (the previous contents of y are not read: they may be uninitialised)
 __global__ void k_neg(double* __restrict__ y, const double* __restrict__ x, long long n)
 {
@@ -66,10 +61,31 @@ __global__ void k_neg(double* __restrict__ y, const double* __restrict__ x, long
         y[i] = -x[i];
 }
 
-__global__ void k_scale(double* __restrict__ y, double c, long long n)
+// The two-loop recursion with its coefficients in device memory, so that its
+// dot products need no host round trip: sc = {dot, ys[m], yy, alpha[m]}.
+// First loop:  alpha_j = dot / ys_j (kept for the second loop); d = -alpha_j y_j + d.
+__global__ void k_loop1(double* __restrict__ d, const double* __restrict__ yj, double* __restrict__ sc, int j, int m,
+                        long long n)
 {
+    const double a = sc[0] / sc[1 + j];
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc[2 + m + j] = a;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        y[i] *= c;
+        d[i] = -a * yj[i] + 1.0 * d[i];
+}
+// d *= ys / yy of the newest pair (slot j)
+__global__ void k_scale_pair(double* __restrict__ d, const double* __restrict__ sc, int j, int m, long long n)
+{
+    const double c = sc[1 + j] / sc[1 + m];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] *= c;
+}
+// Second loop: beta = dot / ys_j; d = (alpha_j - beta) s_j + d.
+__global__ void k_loop2(double* __restrict__ d, const double* __restrict__ sj, const double* __restrict__ sc, int j,
+                        int m, long long n)
+{
+    const double c = sc[2 + m + j] - sc[0] / sc[1 + j];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] = c * sj[i] + 1.0 * d[i];
 }
 
 // z = x + c * y
@@ -87,7 +103,8 @@ struct fwi_lbfgs {
     fwi_lbfgs_param p{};
     double *x = nullptr, *xp = nullptr, *g = nullptr, *gp = nullptr, *d = nullptr, *S = nullptr, *Y = nullptr;
     double *part = nullptr, *dot = nullptr;
-    std::vector<double> alpha, ys_mem, step_arr;
+    double* sc = nullptr;          // device scalars of the two-loop recursion: dot, ys[m], yy, alpha[m]
+    std::vector<double> step_arr;
     int k = 1, end = 0, count = 0, evaluations = 0, state = -1;
     double step = 0, fx = 0, finit = 0, dginit = 0, dgtest = 0;
     cudaStream_t st = nullptr;
@@ -103,6 +120,14 @@ unsigned vec_blocks(long long n) { return (unsigned)std::min<long long>((n + 255
 unsigned vec_blocks(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 4 * 152 * 8); }
 #endif
 
+// a . b into the device scalar *dev (no host wait)
+void dot_dev(fwi_lbfgs* L, const double* a, const double* b, double* dev)
+{
+    FWI_LAUNCH(k_dot_part, DOT_BLOCKS, DOT_THREADS, 0, L->st, a, b, L->n, L->part);
+    FWI_LAUNCH(k_dot_final, 1, 32, 0, L->st, L->part, DOT_BLOCKS, dev);
+}
+
+// a . b on the host (one wait): for the line-search decisions
 int dot(fwi_lbfgs* L, const double* a, const double* b, double* out)
 {
     FWI_LAUNCH(k_dot_part, DOT_BLOCKS, DOT_THREADS, 0, L->st, a, b, L->n, L->part);
@@ -171,13 +196,12 @@ fwi_lbfgs* fwi_lbfgs_create(long long n, const fwi_lbfgs_param* param, int* stat
         if (cudaMalloc(b, sizeof(double) * n) != cudaSuccess) { cudaGetLastError(); return bail(FWI_ERR_NOMEM, L); }
     if (cudaMalloc(&L->S, sizeof(double) * n * p.m) != cudaSuccess ||
         cudaMalloc(&L->Y, sizeof(double) * n * p.m) != cudaSuccess ||
-        cudaMalloc(&L->part, sizeof(double) * DOT_BLOCKS) != cudaSuccess || cudaMalloc(&L->dot, sizeof(double)) != cudaSuccess) {
+        cudaMalloc(&L->part, sizeof(double) * DOT_BLOCKS) != cudaSuccess || cudaMalloc(&L->dot, sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&L->sc, sizeof(double) * (2 + 2 * (size_t)p.m)) != cudaSuccess) {
         cudaGetLastError();
         return bail(FWI_ERR_NOMEM, L);
     }
     if (cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking) != cudaSuccess) { cudaGetLastError(); return bail(FWI_ERR_CUDA, L); }
-    L->alpha.assign(p.m, 0.0);
-    L->ys_mem.assign(p.m, 0.0);
     L->step_arr.assign(p.max_iterations + 2, 0.0);
     if (status) *status = FWI_OK;
     return L;
@@ -186,7 +210,7 @@ fwi_lbfgs* fwi_lbfgs_create(long long n, const fwi_lbfgs_param* param, int* stat
 void fwi_lbfgs_destroy(fwi_lbfgs* L)
 {
     if (!L) return;
-    double* bufs[] = {L->x, L->xp, L->g, L->gp, L->d, L->S, L->Y, L->part, L->dot};
+    double* bufs[] = {L->x, L->xp, L->g, L->gp, L->d, L->S, L->Y, L->part, L->dot, L->sc};
     for (double* b : bufs) if (b) cudaFree(b);
     if (L->st) cudaStreamDestroy(L->st);
     delete L;
@@ -258,17 +282,18 @@ int fwi_lbfgs_next(fwi_lbfgs* L, double* x, double f, const double* g, int g_on_
         *state = L->state;
         return FWI_OK;
     }
-    // correction pair and two-loop recursion (MBotOpt.c:188-213)
+    // correction pair and two-loop recursion (MBotOpt.c:188-213); its
+    // coefficients stay on the device (k_loop1, k_scale_pair, k_loop2), so
+    // the recursion needs no host wait
     const int m = L->p.m;
+    const int newest = L->end;
     double* s = L->S + (size_t)L->end * L->n;
     double* y = L->Y + (size_t)L->end * L->n;
     const unsigned nb = vec_blocks(L->n);
     FWI_LAUNCH(k_xpcy, nb, 256, 0, L->st, s, L->x, L->xp, -1.0, L->n);
     FWI_LAUNCH(k_xpcy, nb, 256, 0, L->st, y, L->g, L->gp, -1.0, L->n);
-    double ys, yy;
-    LB_CK(dot(L, y, s, &ys));
-    LB_CK(dot(L, y, y, &yy));
-    L->ys_mem[L->end] = ys;
+    dot_dev(L, y, s, L->sc + 1 + newest);                  // ys of the newest pair
+    dot_dev(L, y, y, L->sc + 1 + m);                       // yy
     const int bound = (m <= L->k) ? m : L->k;
     ++L->k;
     L->end = (L->end + 1) % m;
@@ -276,20 +301,16 @@ int fwi_lbfgs_next(fwi_lbfgs* L, double* x, double f, const double* g, int g_on_
     int j = L->end;
     for (int i = 0; i < bound; ++i) {
         j = (j + m - 1) % m;
-        double a;
-        LB_CK(dot(L, L->S + (size_t)j * L->n, L->d, &a));
-        a /= L->ys_mem[j];
-        L->alpha[j] = a;
-        FWI_LAUNCH(k_axpby, nb, 256, 0, L->st, L->d, L->Y + (size_t)j * L->n, -a, 1.0, L->n);
+        dot_dev(L, L->S + (size_t)j * L->n, L->d, L->sc);
+        FWI_LAUNCH(k_loop1, nb, 256, 0, L->st, L->d, L->Y + (size_t)j * L->n, L->sc, j, m, L->n);
     }
-    FWI_LAUNCH(k_scale, nb, 256, 0, L->st, L->d, ys / yy, L->n);
+    FWI_LAUNCH(k_scale_pair, nb, 256, 0, L->st, L->d, L->sc, newest, m, L->n);
     for (int i = 0; i < bound; ++i) {
-        double beta;
-        LB_CK(dot(L, L->Y + (size_t)j * L->n, L->d, &beta));
-        beta /= L->ys_mem[j];
-        FWI_LAUNCH(k_axpby, nb, 256, 0, L->st, L->d, L->S + (size_t)j * L->n, L->alpha[j] - beta, 1.0, L->n);
+        dot_dev(L, L->Y + (size_t)j * L->n, L->d, L->sc);
+        FWI_LAUNCH(k_loop2, nb, 256, 0, L->st, L->d, L->S + (size_t)j * L->n, L->sc, j, m, L->n);
         j = (j + 1) % m;
     }
+    LB_CU(cudaGetLastError());
     L->step = (L->k < 4) ? 0.2 : 0.5 * (L->step_arr[L->k - 1] + L->step_arr[L->k - 2]);
     LB_CK(start_line_search(L, x));
     *state = L->state;
