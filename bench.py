@@ -15,6 +15,10 @@ imaging, and the FP64 reduction over shots.  Prints one JSON line.
   the misfit and the FP64 gradient.
 * ``roofline``: the dominant kernel (the fused backward step) at its
   algorithmic 36 B per physical cell-step against the measured HBM copy peak.
+* ``c3``: the 256-shot uneven batch (600 x 2000, records of 3000-6000 steps,
+  off-end spreads of 200-1200 receivers) measured in the same run: throughput,
+  backward roofline, plain per-shot ratio and the FP64 check of its shortest
+  shot (single-GPU runs of the default workload; ``--skip c3`` leaves it out).
 * ``cpu_baseline``: the reference's CPU path on the machine's host cores on a
   bounded sample of the same workload (--cpu-shots shots, the first
   --cpu-steps time steps), scaled linearly; ``kind`` "reference" when the reference's own
@@ -69,7 +73,7 @@ def parse():
     ap.add_argument("--snap-precision", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--hbm-budget-mb", type=int, default=0, help="budget of --store auto (0: 90%% of free memory)")
     ap.add_argument("--fd-order", type=int, default=4, choices=[4, 8], help="4: the reference's; 8: the extension")
-    ap.add_argument("--skip", default="", help="comma list of: e2e,plain,cpu,strips,tune")
+    ap.add_argument("--skip", default="", help="comma list of: e2e,plain,cpu,strips,tune,c3")
     return ap.parse_args()
 
 
@@ -282,6 +286,90 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def extra_leg(name, args, local, stream):
+    """A second workload measured in the same run (single GPU): its own
+    throughput (CUDA events on the engine's stream, 3 warm-up gradients, one
+    timed), backward roofline, plain per-shot ratio over 4 shots and the
+    gradient of its shortest shot against the FP64 oracle (a bounded CPU
+    check).  Reported as an extra key of the main line."""
+    import numpy as np
+    import torch
+    import fwigpu
+    import tuning
+    import workloads
+    cfgkw, vtrue, vstart, shots = workloads.build(name)
+    cells = float(cfgkw["nx"] * cfgkw["nz"])
+    step_cells = sum(s.nt for s in shots) * cells
+    with fwigpu.Engine(fwigpu.make_config(**cfgkw, device=local, use_graph=1)) as eng:
+        eng.set_stream(stream.cuda_stream)
+        eng.set_shots(shots)
+        tune = tuning.autotune(eng, shots, vstart)
+        eng.set_model(vtrue)
+        obs = eng.forward()
+        eng.set_observed(obs)
+        eng.set_model(vstart)
+        for _ in range(3):
+            eng.gradient(keep_on_device=True)
+        torch.cuda.synchronize()
+        clk = Clocks(local)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.gradient(keep_on_device=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        clocks = clk.stop()
+        ms = e0.elapsed_time(e1)
+        st = eng.stats()
+    nt_max = max(s.nt for s in shots)
+    peak, peak_kind = peaks()
+    bwd_launch_ms = st["ms_backward"] / nt_max
+    achieved = BWD_BYTES * step_cells / nt_max / (bwd_launch_ms / 1e3) / 1e9
+    out = {"workload": describe(argparse.Namespace(**dict(vars(args), workload=name)), cfgkw, shots)["workload"],
+           "value": len(shots) / (ms / 1e3), "unit": UNIT,
+           "ms_per_step": ms, "steps": 1, "warmup": 3, "gcell_steps_per_s": 3.0 * step_cells / (ms / 1e3) / 1e9,
+           "nt": [min(s.nt for s in shots), nt_max], "receivers": [min(s.nr for s in shots), max(s.nr for s in shots)],
+           "clocks": clocks, "tuning": tune["tuning"],
+           "roofline": {"kernel": "k_backward", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_kind": peak_kind, "avg_launch_ms": bwd_launch_ms}}
+    # plain per-shot path on 4 shots of the batch
+    k = 4
+    with fwigpu.Engine(fwigpu.make_config(**dict(cfgkw, nt_max=max(s.nt for s in shots[:k])), device=local,
+                                          plain_per_shot=1)) as pe:
+        pe.set_stream(stream.cuda_stream)
+        pe.set_shots(shots[:k])
+        pe.set_model(vstart)
+        pe.set_observed(obs[:pe.nsamples])
+        pe.gradient(keep_on_device=True)
+        e0.record(stream)
+        pe.gradient(keep_on_device=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain = k / (e0.elapsed_time(e1) / 1e3)
+    out["plain"] = {"shots": k, "value": plain, "batched_over_plain": out["value"] / plain}
+    # accuracy: the shortest shot against the FP64 oracle
+    if "cpu" not in set(filter(None, args.skip.split(","))):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        i = min(range(len(shots)), key=lambda q: shots[q].nt)
+        s0 = shots[i]
+        o64 = O.Oracle("f64")
+        ocfg = O.make_config(nx=cfgkw["nx"], nz=cfgkw["nz"], npml=cfgkw["npml"], nt=s0.nt, dx=cfgkw["dx"],
+                             dz=cfgkw["dz"], dt=cfgkw["dt"], free_surface=1, jump=cfgkw["jump"],
+                             nthreads=os.cpu_count() or 1)
+        osh = oracle_shots(O, o64, [s0], cfgkw["dx"], cfgkw["dz"], s0.nt)[0]
+        ob = o64.forward(ocfg, vtrue, osh).astype(np.float32)
+        _, g64, _ = o64.gradient(ocfg, vstart, [osh], [ob])
+        with fwigpu.Engine(fwigpu.make_config(**dict(cfgkw, nt_max=s0.nt), device=local)) as e1_:
+            e1_.set_shots([s0])
+            e1_.set_model(vstart)
+            e1_.set_observed(ob)
+            g = e1_.gradient()[1]
+        out["accuracy"] = {"grad_rel_err_vs_fp64": float(np.linalg.norm(g - g64) / np.linalg.norm(g64)),
+                           "sample": f"the shortest shot ({s0.nt} steps, {s0.nr} receivers), workload grid"}
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -487,6 +575,13 @@ def run_ours(args):
         line["accuracy"] = {"grad_rel_err_vs_fp64": r["grad_rel_err"],
                             "cpu_fp32_grad_rel_err_vs_fp64": r["grad_rel_err_cpu_fp32"],
                             "sample": f"1 shot, {r['nt']} steps, workload grid"}
+    # the uneven-batch configuration beside the default one (single GPU only)
+    if args.workload == "c2" and world == 1 and "c3" not in skip:
+        eng.close()
+        try:
+            line["c3"] = extra_leg("c3", args, local, stream)
+        except Exception as e:                                  # the main line stands on its own
+            line["c3"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     eng.close()     # idempotent
