@@ -19,6 +19,8 @@ imaging, and the FP64 reduction over shots.  Prints one JSON line.
   off-end spreads of 200-1200 receivers) measured in the same run: throughput,
   backward roofline, plain per-shot ratio and the FP64 check of its shortest
   shot (single-GPU runs of the default workload; ``--skip c3`` leaves it out).
+* ``aux``: sfbandpass and grad_precond_new5 through the C ABI against the
+  reference's own compiled routines (bit-identical outputs, wall times).
 * ``cpu_baseline``: the reference's CPU path on the machine's host cores on a
   bounded sample of the same workload (--cpu-shots shots, the first
   --cpu-steps time steps), scaled linearly; ``kind`` "reference" when the reference's own
@@ -73,7 +75,7 @@ def parse():
     ap.add_argument("--snap-precision", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--hbm-budget-mb", type=int, default=0, help="budget of --store auto (0: 90%% of free memory)")
     ap.add_argument("--fd-order", type=int, default=4, choices=[4, 8], help="4: the reference's; 8: the extension")
-    ap.add_argument("--skip", default="", help="comma list of: e2e,plain,cpu,strips,tune,c3")
+    ap.add_argument("--skip", default="", help="comma list of: e2e,plain,cpu,strips,tune,c3,aux")
     return ap.parse_args()
 
 
@@ -284,6 +286,47 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def aux_leg(local):
+    """The routines around the gradient on C2-sized data, each through the C
+    ABI (host buffers in and out, device buffers allocated per call) against
+    the reference's own compiled routine on one host core (the reference runs
+    them serially): sfbandpass on one shot record of 1700 traces x 4000
+    samples, grad_precond_new5 on a 560 x 1700 gradient.  Outputs are compared
+    bit for bit."""
+    import numpy as np
+    import fwigpu
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    ref = O.RefAux() if O.RefAux.available() else O.AuxOracle()
+    kind = "reference" if O.RefAux.available() else "port"
+    rng = np.random.default_rng(7)
+    out = {}
+    traces = rng.standard_normal((1700, 4000)).astype(np.float32)
+    bp = (0.0008, 0, 6, 6, 10.0, 3.0)                       # dt, zero phase, orders, fhi, flo
+    grad = (rng.standard_normal((560, 1700)) * 1e-3).astype(np.float32)
+    bottom = rng.integers(0, 40, 1700).astype(np.int32)
+    pc = (0.95, 20, 3, 15, 2, 1.0)                           # perc, rect1, repeat1, rect2, repeat2, alpha
+    for name, gpu, cpu in (
+            ("bandpass", lambda: fwigpu.bandpass(traces, *bp), lambda: ref.bandpass(traces, *bp)),
+            ("grad_precond", lambda: fwigpu.grad_precond(grad, *pc, bottom),
+             lambda: ref.grad_precond(grad, *pc, bottom))):
+        gpu()                                                # first call: module load
+        t0 = time.perf_counter()
+        g_out = gpu()
+        t_gpu = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        c_out = cpu()
+        t_cpu = time.perf_counter() - t0
+        out[name] = {"gpu_ms": t_gpu * 1e3, "cpu_ms": t_cpu * 1e3, "cpu_kind": kind, "cpu_threads": 1,
+                     "speedup": t_cpu / t_gpu, "bit_identical": bool(np.array_equal(g_out, c_out))}
+    out["bandpass"]["data"] = "1700 traces x 4000 samples, zero phase, orders 6/6, 3-10 Hz"
+    out["grad_precond"]["data"] = "560 x 1700, perc 0.95, triangle 20 x3 then 15 x2"
+    out["note"] = ("wall time of one call each: the GPU's includes the host-device copies and the per-call device "
+                   "allocations of the C ABI")
+    return out
 
 
 def extra_leg(name, args, local, stream):
@@ -575,6 +618,11 @@ def run_ours(args):
         line["accuracy"] = {"grad_rel_err_vs_fp64": r["grad_rel_err"],
                             "cpu_fp32_grad_rel_err_vs_fp64": r["grad_rel_err_cpu_fp32"],
                             "sample": f"1 shot, {r['nt']} steps, workload grid"}
+    if rank == 0 and world == 1 and "aux" not in skip:
+        try:
+            line["aux"] = aux_leg(local)
+        except Exception as e:
+            line["aux"] = {"error": f"{type(e).__name__}: {e}"}
     # the uneven-batch configuration beside the default one (single GPU only)
     if args.workload == "c2" and world == 1 and "c3" not in skip:
         eng.close()
