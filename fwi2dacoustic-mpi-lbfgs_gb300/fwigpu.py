@@ -77,6 +77,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.fwi_forward.argtypes = [P, C.POINTER(F)]
     lib.fwi_backward.argtypes = [P, C.POINTER(F), C.POINTER(D)]
     lib.fwi_gradient.argtypes = [P, C.POINTER(D), C.POINTER(D)]
+    lib.fwi_gradient_obs.argtypes = [P, C.POINTER(F), C.POINTER(D), C.POINTER(D)]
     lib.fwi_gradient_f32.argtypes = [P, C.POINTER(D), C.POINTER(F)]
     lib.fwi_grad_device.argtypes = [P]
     lib.fwi_grad_device.restype = P
@@ -255,15 +256,23 @@ class Engine:
         self._check(self.lib.fwi_backward(self.ctx, _fp(res), _dp(grad)), "fwi_backward")
         return grad
 
-    def gradient(self, keep_on_device=False, out=None):
+    def gradient(self, keep_on_device=False, out=None, observed=None):
         """Misfit and dJ/dv.  ``out`` (float64 [nz][nx], e.g. pinned memory)
-        receives the gradient; ``keep_on_device`` leaves it on the device."""
+        receives the gradient; ``keep_on_device`` leaves it on the device.
+        ``observed`` (the traces of set_observed, best in pinned memory) sets
+        the observed traces in the same call, uploaded beside the forward
+        phase (fwi_gradient_obs)."""
         mis = np.zeros(2, np.float64)
         grad = None
         if not keep_on_device:
             grad = out if out is not None else np.zeros((self.cfg.nz, self.cfg.nx), np.float64)
             assert grad.dtype == np.float64 and grad.size == self.cfg.nz * self.cfg.nx and grad.flags.c_contiguous
-        self._check(self.lib.fwi_gradient(self.ctx, _dp(mis), _dp(grad)), "fwi_gradient")
+        if observed is None:
+            self._check(self.lib.fwi_gradient(self.ctx, _dp(mis), _dp(grad)), "fwi_gradient")
+        else:
+            obs = np.ascontiguousarray(observed, np.float32).ravel()
+            assert obs.size == self.nsamples, (obs.size, self.nsamples)
+            self._check(self.lib.fwi_gradient_obs(self.ctx, _fp(obs), _dp(mis), _dp(grad)), "fwi_gradient_obs")
         return float(mis[1]), grad
 
     def grad_device_ptr(self) -> int:

@@ -188,6 +188,17 @@ int fwi_backward(fwi_ctx *ctx, const float *residual, double *grad_out);
  * device (fwi_grad_device). */
 int fwi_gradient(fwi_ctx *ctx, double *misfit, double *grad_out);
 
+/* fwi_set_observed followed by fwi_gradient in one call, with the upload of
+ * obs (layout of fwi_set_observed) running on a copy stream beside the
+ * forward phase, which does not read it; the misfit phase waits for it.
+ * From page-locked host memory the copy overlaps the forward modelling; from
+ * pageable memory it is staged first, as fwi_set_observed's is.  The upload
+ * has completed when the call returns, on success and on error alike, so obs
+ * is the caller's again; afterwards the observed traces are set as if by
+ * fwi_set_observed.  One call per iteration of the reference's loop with
+ * fresh data (the per-shot msf->obs0 read at fwi_2d.c:342). */
+int fwi_gradient_obs(fwi_ctx *ctx, const float *obs, double *misfit, double *grad_out);
+
 /* Misfit of fwi_gradient (the misfit pool of the reference's fwi_init,
  * fwi_2d.c:194-213, par_xcorr1d header.h:309-315). */
 #define FWI_MISFIT_L2 0
@@ -256,10 +267,12 @@ int fwi_set_tuning(fwi_ctx *ctx, const fwi_tuning *tuning);
 /* The tuning in use, every field resolved (no zeros). */
 int fwi_get_tuning(const fwi_ctx *ctx, fwi_tuning *out);
 /* Times `steps` forward and `steps` backward time steps of the current shot
- * batch (after fwi_set_shots and fwi_set_model) and returns the average
+ * batch (after fwi_set_shots and fwi_set_model), captured into CUDA graphs
+ * and replayed as the gradient replays its phases, and returns the average
  * device time of one step of each; the fields they compute are discarded
  * (a following fwi_backward needs a new fwi_forward).  For sweeps over
- * fwi_tuning; the 8th-order path has nothing to tune but the serial flag. */
+ * fwi_tuning; the 8th-order path has nothing to tune but the serial flag and
+ * the priority. */
 int fwi_time_steps(fwi_ctx *ctx, int steps, double *ms_forward_step, double *ms_backward_step);
 const char *fwi_status_string(int status);
 const char *fwi_last_error(const fwi_ctx *ctx);   /* detail of the last failure */

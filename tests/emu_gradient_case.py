@@ -3,7 +3,8 @@ against the FP64 oracle; run by test_emu_sanitized.py in a child process
 with AddressSanitizer and UBSan preloaded and FWI_LIB pointing at
 libfwiemu.so.  Arguments: free surface, nt, nx, nz [, nseg [, fd_order [,
 x shift, z shift of the tile grid (fwi_tuning)]]].
-Prints one JSON line {J, J64, grad_rel, syn_rel}.  With nseg > 0 the same gradient is also taken with checkpoints
+Prints one JSON line {J, J64, grad_rel, syn_rel, obs_call_same} (the last:
+fwi_gradient_obs returns fwi_gradient's result bit for bit).  With nseg > 0 the same gradient is also taken with checkpoints
 (FWI_STORE_SNAPSHOTS, nseg segments) in FP32 and FP16 storage (BF16 shares
 the FP16 path but for its rounding) and the line adds {snap_f32_rel,
 snap_f16_rel} (against FP64) and snap_f32_vs_strips."""
@@ -44,10 +45,12 @@ def main(fs, nt, nx=150, nz=90, nseg=0, order=4, xshift=0, zshift=0):
         j, gg, _ = o64.gradient(case.oracle_cfg_for(len(s.wav)), case.vel, [s], [ob])
         J64 += j
         g64 += gg
-    out = {"J": J, "J64": J64, "grad_rel": rel(g, g64), "syn_rel": syn_rel}
+    flat = np.concatenate([o.ravel() for o in obs])
+    J2, g2 = e.gradient(observed=flat.copy())            # fwi_gradient_obs: the same gradient
+    out = {"J": J, "J64": J64, "grad_rel": rel(g, g64), "syn_rel": syn_rel,
+           "obs_call_same": bool(J2 == J and np.array_equal(g2, g))}
     if nseg:
         import fwigpu
-        flat = np.concatenate([o.ravel() for o in obs])
         for prec in ("f32", "f16"):
             c = case.ecfg
             cfg = fwigpu.make_config(c.nx, c.nz, c.dx, c.dz, c.dt, c.nt_max, npml=c.npml,
