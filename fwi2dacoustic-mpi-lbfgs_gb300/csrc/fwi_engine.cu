@@ -350,7 +350,7 @@ void join_classes(fwi_ctx* x)
 
 // The general-tile class cls (0 = x-general, 1 = z-general, 2 = corners) in
 // the variant compiled for MB resident blocks per SM.  z-only tiles never
-// touch srx, the last member of BwdSmem.
+// touch su, srx or the x psi sites, the members of BwdSmem from su on.
 template <int MB>
 void launch_fwd_gen(int cls, dim3 grid, dim3 block, cudaStream_t cs, const StepParams& P)
 {
@@ -362,7 +362,7 @@ template <int MB>
 void launch_bwd_edge(int cls, dim3 grid, dim3 block, cudaStream_t cs, const StepParams& P)
 {
     if (cls == 0) FWI_LAUNCH((k_bwd_edge<true, false, MB>), grid, block, sizeof(BwdSmem), cs, P);
-    if (cls == 1) FWI_LAUNCH((k_bwd_edge<false, true, MB>), grid, block, offsetof(BwdSmem, srx), cs, P);
+    if (cls == 1) FWI_LAUNCH((k_bwd_edge<false, true, MB>), grid, block, offsetof(BwdSmem, su), cs, P);
     if (cls == 2) FWI_LAUNCH((k_bwd_edge<true, true, MB>), grid, block, sizeof(BwdSmem), cs, P);
 }
 // Dynamic shared memory limits of the backward variants.
@@ -493,7 +493,7 @@ long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
     P.shot_base = lo;
     if (x->M == 4) return launch_bwd_step8(x, P, n);
     fork_classes(x);
-    // z-only tiles never touch srx (the last member of BwdSmem)
+    // z-only tiles never touch the members of BwdSmem from su on
     const int2* gen = P.gen_tiles;
     for (int k = 0; k < 3; ++k) {
         const int cls = class_order(x)[k];
@@ -965,7 +965,7 @@ fwi_tuning default_tuning(const fwi_ctx* x)
     t.x_first = (int)round_up(std::max(8, np + 5), 4);
     t.z_first = x->cfg.free_surface ? 8 : (int)round_up(std::max(8, np + 5), R);
     t.fwd_gen_blocks = 4;
-    t.bwd_gen_blocks = 4;
+    t.bwd_gen_blocks = 3;           // 80 registers: the psi-site tables made the 64-register variant 11% slower
     t.fwd_int_blocks = 6;
     t.bwd_int_blocks = 4;
     t.class_order = 1;

@@ -350,6 +350,52 @@ __device__ __forceinline__ PsiSite psi_vz(const StepParams& P, int row, int c)
 // psi value of a site (0 where there is none)
 __device__ __forceinline__ float psi_load(const float* psr, const PsiSite& t) { return t.idx >= 0 ? __ldcg(GP(psr + t.idx)) : 0.f; }
 
+// The psi sites of a general tile, one entry per row (z sites) or column (x
+// sites) within its reach, built once per block by psi_v / psi_vz at column 0
+// and psi_u / psi_ux at row 0: off is the site's offset there (-1: no site)
+// and a, b its recursion coefficients.  A z site of column c is off + c (c in
+// [0, pnx)); an x site of row r is off + r (np + 1) for u and off + r np for
+// ux (r in [0, pnz)).  The tile bodies read one entry instead of deciding the
+// site and loading its coefficients per element.
+struct PsiRowSite {
+    int off;
+    float a, b;
+    int pad;
+};
+struct ZSiteTab {
+    PsiRowSite zvz[TZ + 6];    // vz cells, rows z0-3 .. z0+TZ+2
+    PsiRowSite zv[TZ + 3];     // v positions, rows z0-1 .. z0+TZ+1
+};
+struct XSiteTab {
+    PsiRowSite xux[RXW];       // ux cells, columns x0-3 .. x0+TX+2
+    PsiRowSite xu[UW];         // u positions, columns x0-1 .. x0+TX+1
+};
+__device__ __forceinline__ PsiRowSite row_site(const StepParams& P, const PsiSite& t, int axis)
+{
+    // pmlc holds a0x b0x a1x b1x a0z b0z a1z b1z, 2 npml + 1 each
+    const int n2 = 2 * P.g.npml + 1;
+    if (t.idx < 0) return {-1, 0.f, 0.f, 0};
+    const float* base = P.pmlc + (axis * 4 + t.side * 2) * n2;
+    return {t.idx, *GP(base + t.node), *GP(base + n2 + t.node), 0};
+}
+// Fills the tables a tile of class (GX, GZ) at (x0, z0) reads; a barrier must
+// follow before they are read.
+template <bool GX, bool GZ>
+__device__ __forceinline__ void fill_sites(const StepParams& P, int x0, int z0, ZSiteTab& tz, XSiteTab& tx)
+{
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    if (GZ)
+        for (int i = tid; i < 2 * TZ + 9; i += NTH) {
+            if (i < TZ + 6) tz.zvz[i] = row_site(P, psi_vz(P, z0 - 3 + i, 0), 1);
+            else tz.zv[i - (TZ + 6)] = row_site(P, psi_v(P, z0 - 1 + (i - (TZ + 6)), 0), 1);
+        }
+    if (GX)
+        for (int i = tid; i < RXW + UW; i += NTH) {
+            if (i < RXW) tx.xux[i] = row_site(P, psi_ux(P, 0, x0 - 3 + i), 0);
+            else tx.xu[i - RXW] = row_site(P, psi_u(P, 0, x0 - 1 + (i - RXW)), 0);
+        }
+}
+
 // u = staggered d/dx of p at u-position j (fwi_2d.c:775-784); p[row][col]
 // is sp[base + col] (base = row offset - x0 + HX, an integer, so no pointer
 // leaves the array).
@@ -506,19 +552,15 @@ __device__ __forceinline__ void gather_residuals(const StepParams& P, int rb, in
 // pnx skip their work (uniform per warp).
 template <bool GX, bool GZ>
 __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd, int s, int x0, int z0,
-                                         float* sp, float* su)
+                                         float* sp, float* su, const ZSiteTab& tbz, const XSiteTab& tbx)
 {
     const Geo& g = P.g;
     const Coef& cf = P.c;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int n2 = 2 * g.npml + 1;
+    const int np = g.npml;
     const long long so = (long long)s * g.fstride;
     const float* __restrict__ psr = P.psr + (long long)s * P.pl.stride;
     float* __restrict__ psw = P.psw + (long long)s * P.pl.stride;
-    const float* a0x = P.pmlc;          const float* b0x = a0x + n2;
-    const float* a1x = a0x + 2 * n2;    const float* b1x = a0x + 3 * n2;
-    const float* a0z = a0x + 4 * n2;    const float* b0z = a0x + 5 * n2;
-    const float* a1z = a0x + 6 * n2;    const float* b1z = a0x + 7 * n2;
 
     // u at positions j in [x0-1, x0+TX+1], rows [z0, z0+TZ); the psi entries
     // of the x-general column halves are read first
@@ -532,7 +574,8 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                 const int jj = tx + BX * h;
                 const bool gen = jj < UW && !(GZ && (row < 0 || row >= g.pnz)) && x_window_general(g, x0 - 1 + BX * h, BX) &&
                                  !x_window_outside(x0 - 1 + BX * h, BX, 0, g.pnx);
-                pu[k][h] = gen ? psi_load(psr, psi_u(P, row, x0 - 1 + jj)) : 0.f;
+                const int off = gen ? tbx.xu[jj].off : -1;
+                pu[k][h] = off >= 0 ? __ldcg(GP(psr + off + row * (np + 1))) : 0.f;
             }
         }
     }
@@ -557,12 +600,10 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                 u = 0.f;
             } else {
                 u = u_edge(sp, pbase, j, g.pnx, cf);
-                const PsiSite t = psi_u(P, row, j);                        // fwi_2d.c:790-794
-                if (t.idx >= 0) {
-                    const float* ca = t.side ? a1x : a0x;
-                    const float* cb = t.side ? b1x : b0x;
-                    const float ps = *GP(cb + t.node) * pu[k][h] + *GP(ca + t.node) * u;
-                    if (jj >= 1 && jj <= TX) *GP(psw + t.idx) = ps;
+                const PsiRowSite e = tbx.xu[jj];                             // fwi_2d.c:790-794
+                if (e.off >= 0) {
+                    const float ps = e.b * pu[k][h] + e.a * u;
+                    if (jj >= 1 && jj <= TX) *GP(psw + e.off + row * (np + 1)) = ps;
                     u += ps;
                 }
             }
@@ -584,8 +625,10 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
         if (GX && (x0 + BX * h >= g.pnx || x0 + BX * h + BX <= 0)) continue;   // column half outside the grid
         const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);        // this half needs the x-general formulas
         const int cl = tx + BX * h, c = x0 + cl;
+        const bool cin = !GX || (c >= 0 && c < g.pnx);                      // z sites exist in grid columns only
         // every global operand of this column segment first: K, p^{it-1} and the psi entries
         float kq[R], po[R], pvv[R + 3], pux[R], pvz[R];
+        const int xoff = gxc ? tbx.xux[cl + 3].off : -1;                     // the ux site of column c
         #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int row = r0 + i;
@@ -593,11 +636,15 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             const long long o = (long long)row * g.ld + c;
             kq[i] = inside ? __ldg(GP(K + o)) : 0.f;
             po[i] = inside ? *GP(pold + o) : 0.f;
-            pux[i] = (gxc && inside) ? psi_load(psr, psi_ux(P, row, c)) : 0.f;
-            pvz[i] = (gzw && inside) ? psi_load(psr, psi_vz(P, row, c)) : 0.f;
+            pux[i] = (inside && xoff >= 0) ? __ldcg(GP(psr + xoff + row * np)) : 0.f;
+            const int zoff = (gzw && inside) ? tbz.zvz[r0l + i + 3].off : -1;
+            pvz[i] = zoff >= 0 ? __ldcg(GP(psr + zoff + c)) : 0.f;
         }
         #pragma unroll
-        for (int k = 0; k < R + 3; ++k) pvv[k] = gzw ? psi_load(psr, psi_v(P, r0 - 1 + k, c)) : 0.f;
+        for (int k = 0; k < R + 3; ++k) {
+            const int off = (gzw && cin) ? tbz.zv[r0l + k].off : -1;
+            pvv[k] = off >= 0 ? __ldcg(GP(psr + off + c)) : 0.f;
+        }
 
         float pc[R + 6];
         #pragma unroll
@@ -622,12 +669,10 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                 } else {
                     v = 0.f;
                 }
-                const PsiSite t = psi_v(P, kv, c);                        // fwi_2d.c:816-817 (v0: top, all sides)
-                if (t.idx >= 0) {
-                    const float* ca = t.side ? a1z : a0z;
-                    const float* cb = t.side ? b1z : b0z;
-                    const float ps = *GP(cb + t.node) * pvv[k] + *GP(ca + t.node) * v;
-                    if (k >= 1 && k <= R && kv < g.pnz) *GP(psw + t.idx) = ps;
+                const PsiRowSite e = tbz.zv[r0l + k];                       // fwi_2d.c:816-817 (v0: top, all sides)
+                if (e.off >= 0 && cin) {
+                    const float ps = e.b * pvv[k] + e.a * v;
+                    if (k >= 1 && k <= R && kv < g.pnz) *GP(psw + e.off + c) = ps;
                     v += ps;
                 }
             }
@@ -674,23 +719,17 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
             }
             #undef UR
             const bool inside = (!GZ || row < g.pnz) && (!GX || (c >= 0 && c < g.pnx));
-            if (gxc && inside) {
-                const PsiSite t = psi_ux(P, row, c);                      // fwi_2d.c:838-842
-                if (t.idx >= 0) {
-                    const float* ca = t.side ? a1x : a0x;
-                    const float* cb = t.side ? b1x : b0x;
-                    const float ps = *GP(cb + t.node) * pux[i] + *GP(ca + t.node) * ux;
-                    *GP(psw + t.idx) = ps;
-                    ux += ps;
-                }
+            if (inside && xoff >= 0) {                                    // fwi_2d.c:838-842
+                const PsiRowSite e = tbx.xux[cl + 3];
+                const float ps = e.b * pux[i] + e.a * ux;
+                *GP(psw + xoff + row * np) = ps;
+                ux += ps;
             }
             if (gzw && inside) {
-                const PsiSite t = psi_vz(P, row, c);                      // fwi_2d.c:860-861
-                if (t.idx >= 0) {
-                    const float* ca = t.side ? a1z : a0z;
-                    const float* cb = t.side ? b1z : b0z;
-                    const float ps = *GP(cb + t.node) * pvz[i] + *GP(ca + t.node) * vz;
-                    *GP(psw + t.idx) = ps;
+                const PsiRowSite e = tbz.zvz[r0l + i + 3];                  // fwi_2d.c:860-861
+                if (e.off >= 0) {
+                    const float ps = e.b * pvz[i] + e.a * vz;
+                    *GP(psw + e.off + c) = ps;
                     vz += ps;
                 }
             }
@@ -715,6 +754,8 @@ __global__ void __launch_bounds__(NTH, MINB) k_fwd_gen(const StepParams P)
 {
     __shared__ __align__(16) float sp[SPH * SPW];
     __shared__ __align__(16) float su[TZ * UWP];
+    __shared__ ZSiteTab tbz;
+    __shared__ XSiteTab tbx;
     const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
     const Geo& g = P.g;
@@ -724,9 +765,10 @@ __global__ void __launch_bounds__(NTH, MINB) k_fwd_gen(const StepParams P)
     stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
     // only active shots are launched; the test waits for nothing the copies need
     if (P.step >= sd.nt) { cp_async_wait(); return; }
+    fill_sites<GX, GZ>(P, x0, z0, tbz, tbx);
     cp_async_wait();
     __syncthreads();
-    fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su);
+    fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su, tbz, tbx);
 }
 
 // Forward step, interior tiles: no edge, CPML or strip cells, so every cell
@@ -817,9 +859,12 @@ __global__ void k_sample(const RecParams Q)
 struct BwdSmem {
     float sq[SPH * SPW];   // b^{m+1} tile + halo
     float sp[SPH * SPW];   // p^{m-1} tile + halo
-    float su[TZ * UWP];    // adjoint ubar, then rebuild u
     float racc[TZ * TX];   // receiver adjoint sources of the tile
-    float srx[TZ * RXP];   // adjoint x-stage input (psi-adjusted b), x-general tiles
+    ZSiteTab tbz;          // z psi sites of the tile
+    // x-general tiles and corners only: z-only tiles are launched without these
+    float su[TZ * UWP];    // adjoint ubar, then rebuild u
+    float srx[TZ * RXP];   // adjoint x-stage input (psi-adjusted b)
+    XSiteTab tbx;          // x psi sites of the tile
 };
 
 // All shared-memory accesses below use integer indices relative to the start
@@ -835,15 +880,13 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
 {
     const Geo& g = P.g;
     const Coef& cf = P.c;
+    const ZSiteTab& tbz = sm.tbz;
+    const XSiteTab& tbx = sm.tbx;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int n2 = 2 * g.npml + 1, pnx = g.pnx, pnz = g.pnz;
+    const int np = g.npml, pnx = g.pnx, pnz = g.pnz;
     const long long so = (long long)s * g.fstride;
     const float* __restrict__ psr = P.psr + (long long)s * P.pl.stride;
     float* __restrict__ psw = P.psw + (long long)s * P.pl.stride;
-    const float* a0x = P.pmlc;          const float* b0x = a0x + n2;
-    const float* a1x = a0x + 2 * n2;    const float* b1x = a0x + 3 * n2;
-    const float* a0z = a0x + 4 * n2;    const float* b0z = a0x + 5 * n2;
-    const float* a1z = a0x + 6 * n2;    const float* b1z = a0x + 7 * n2;
     [[maybe_unused]] constexpr int NS = SPH * SPW, NU = TZ * UWP, NR = TZ * RXP;
 
     // psi entries of both x stages first (independent loads): the ux
@@ -858,11 +901,13 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             #pragma unroll
             for (int h = 0; h < 3; ++h) {
                 const int ii = tx + BX * h, jj = ii;
-                pux[k][h] = (live && ii < RXW && !x_window_outside(x0 - 3 + BX * h, BX, 0, pnx - 1))
-                                ? psi_load(psr, psi_ux(P, row, x0 - 3 + ii)) : 0.f;
+                const int xo = (live && ii < RXW && !x_window_outside(x0 - 3 + BX * h, BX, 0, pnx - 1))
+                                   ? tbx.xux[ii].off : -1;
+                pux[k][h] = xo >= 0 ? __ldcg(GP(psr + xo + row * np)) : 0.f;
                 const bool gen = live && jj < UW && x_window_general(g, x0 - 1 + BX * h, BX) &&
                                  !x_window_outside(x0 - 1 + BX * h, BX, 0, pnx);
-                pu[k][h] = gen ? psi_load(psr, psi_u(P, row, x0 - 1 + jj)) : 0.f;
+                const int uo = gen ? tbx.xu[jj].off : -1;
+                pu[k][h] = uo >= 0 ? __ldcg(GP(psr + uo + row * (np + 1))) : 0.f;
             }
         }
     }
@@ -880,13 +925,11 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 if (ii >= RXW) break;
                 if (x_window_outside(x0 - 3 + BX * h, BX, 0, pnx - 1)) continue;   // stage 2 reads cells 0 .. pnx-1
                 float r = sm.sq[SIDX(qrow + ii, NS)];
-                const PsiSite t = psi_ux(P, row, x0 - 3 + ii);
-                if (t.idx >= 0) {
-                    const float* ca = t.side ? a1x : a0x;
-                    const float* cb = t.side ? b1x : b0x;
+                const PsiRowSite e = tbx.xux[ii];
+                if (e.off >= 0) {
                     const float tt = r + pux[k][h];
-                    r = r + *GP(ca + t.node) * tt;
-                    if (ii >= 3 && ii < 3 + TX) *GP(psw + t.idx) = *GP(cb + t.node) * tt;
+                    r = r + e.a * tt;
+                    if (ii >= 3 && ii < 3 + TX) *GP(psw + e.off + row * np) = e.b * tt;
                 }
                 sm.srx[SIDX(rl * RXP + ii, NR)] = r;
             }
@@ -921,13 +964,11 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 if (j == 0) ub -= cf.ix * sm.srx[SIDX(rbase, NR)];
                 if (j == pnx) ub += cf.ix * sm.srx[SIDX(rbase + pnx - 1, NR)];
                 if (j == pnx - 1) ub -= cf.ix * sm.srx[SIDX(rbase + pnx - 1, NR)];
-                const PsiSite t = psi_u(P, row, j);
-                if (t.idx >= 0) {
-                    const float* ca = t.side ? a1x : a0x;
-                    const float* cb = t.side ? b1x : b0x;
+                const PsiRowSite e = tbx.xu[jj];
+                if (e.off >= 0) {
                     const float tt = ub + pu[k][h];
-                    ub = ub + *GP(ca + t.node) * tt;
-                    if (jj >= 1 && jj <= TX) *GP(psw + t.idx) = *GP(cb + t.node) * tt;
+                    ub = ub + e.a * tt;
+                    if (jj >= 1 && jj <= TX) *GP(psw + e.off + row * (np + 1)) = e.b * tt;
                 }
             }
             sm.su[SIDX(rl * UWP + jj, NU)] = ub;
@@ -947,6 +988,7 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         if (GX && (x0 + BX * h >= pnx || x0 + BX * h + BX <= 0)) continue;   // column half outside the grid
         const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);        // this half needs the x-general formulas
         const int cl = tx + BX * h, c = x0 + cl;
+        const bool zs = gzw && (!GX || (c >= 0 && c < pnx));               // z sites exist in grid columns only
         // every global operand of this column segment first: K, b^{m+2} and the psi entries
         float kq[R], bo[R], prz[R + 6], pvb[R + 3];
         #pragma unroll
@@ -958,9 +1000,15 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
             bo[i] = inside ? *GP(bold + o) : 0.f;
         }
         #pragma unroll
-        for (int k = 0; k < R + 6; ++k) prz[k] = gzw ? psi_load(psr, psi_vz(P, r0 - 3 + k, c)) : 0.f;
+        for (int k = 0; k < R + 6; ++k) {
+            const int off = zs ? tbz.zvz[r0l + k].off : -1;
+            prz[k] = off >= 0 ? __ldcg(GP(psr + off + c)) : 0.f;
+        }
         #pragma unroll
-        for (int k = 0; k < R + 3; ++k) pvb[k] = gzw ? psi_load(psr, psi_v(P, r0 - 1 + k, c)) : 0.f;
+        for (int k = 0; k < R + 3; ++k) {
+            const int off = zs ? tbz.zv[r0l + k].off : -1;
+            pvb[k] = off >= 0 ? __ldcg(GP(psr + off + c)) : 0.f;
+        }
 
         float qc[R + 6];
         #pragma unroll
@@ -969,14 +1017,12 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
         #pragma unroll
         for (int k = 0; k < R + 6; ++k) {
             float r = qc[k];
-            if (gzw) {
-                const PsiSite t = psi_vz(P, r0 - 3 + k, c);
-                if (t.idx >= 0) {
-                    const float* ca = t.side ? a1z : a0z;
-                    const float* cb = t.side ? b1z : b0z;
+            if (zs) {
+                const PsiRowSite e = tbz.zvz[r0l + k];
+                if (e.off >= 0) {
                     const float tt = r + prz[k];
-                    r = r + *GP(ca + t.node) * tt;
-                    if (k >= 3 && k < 3 + R) *GP(psw + t.idx) = *GP(cb + t.node) * tt;
+                    r = r + e.a * tt;
+                    if (k >= 3 && k < 3 + R) *GP(psw + e.off + c) = e.b * tt;
                 }
             }
             rz[k] = r;
@@ -1010,14 +1056,12 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
                 if (kv == pnz) v += cf.iz * rz[k + 1];
                 if (kv == pnz - 1) v -= cf.iz * rz[k + 2];
             }
-            if (gzw) {
-                const PsiSite t = psi_v(P, kv, c);
-                if (t.idx >= 0) {
-                    const float* ca = t.side ? a1z : a0z;
-                    const float* cb = t.side ? b1z : b0z;
+            if (zs) {
+                const PsiRowSite e = tbz.zv[r0l + k];
+                if (e.off >= 0) {
                     const float tt = v + pvb[k];
-                    v = v + *GP(ca + t.node) * tt;
-                    if (k >= 1 && k <= R && kv < pnz) *GP(psw + t.idx) = *GP(cb + t.node) * tt;
+                    v = v + e.a * tt;
+                    if (k >= 1 && k <= R && kv < pnz) *GP(psw + e.off + c) = e.b * tt;
                 }
             }
             vb[k] = v;
@@ -1114,6 +1158,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_bwd_edge(const StepParams P)
         __syncthreads();
         gather_residuals(P, rb, re, (m - 1) / P.jump, sm.racc);
     }
+    fill_sites<GX, GZ>(P, x0, z0, sm.tbz, sm.tbx);
     cp_async_wait();
     __syncthreads();
 

@@ -242,7 +242,7 @@ int fwi_get_stats(const fwi_ctx *ctx, fwi_stats *out);
  *       the fields: fwi_set_tuning then discards the shots and the model,
  *       which must be set again.
  *   fwd_gen_blocks, bwd_gen_blocks: resident blocks per SM the general-tile
- *       kernels are compiled for, 3 or 4 (default 4);
+ *       kernels are compiled for, 3 or 4 (default 4 forward, 3 backward);
  *   fwd_int_blocks: the interior forward kernel, 4 or 6 (default 6);
  *   bwd_int_blocks: the interior backward kernel, 3 or 4 (default 4);
  *   class_order: 1 launches the z-general class first (default), 2 the
