@@ -231,6 +231,7 @@ enum { cudaStreamNonBlocking = 1, cudaEventDisableTiming = 2 };
 enum cudaStreamCaptureMode { cudaStreamCaptureModeThreadLocal };
 enum cudaStreamCaptureStatus { cudaStreamCaptureStatusNone, cudaStreamCaptureStatusActive };
 enum cudaFuncAttribute { cudaFuncAttributeMaxDynamicSharedMemorySize };
+enum cudaDeviceAttr { cudaDevAttrMultiProcessorCount };
 struct cudaDeviceProp { int major = 10, minor = 3; };
 
 inline const char* cudaGetErrorString(cudaError_t e) { return e ? "emulation: not supported" : "no error"; }
@@ -238,6 +239,7 @@ inline cudaError_t cudaGetLastError() { return cudaSuccess; }
 inline cudaError_t cudaPeekAtLastError() { return cudaSuccess; }
 inline cudaError_t cudaStreamIsCapturing(cudaStream_t, cudaStreamCaptureStatus* c) { *c = cudaStreamCaptureStatusNone; return cudaSuccess; }
 inline cudaError_t cudaGetDeviceCount(int* n) { *n = 1; return cudaSuccess; }
+inline cudaError_t cudaDeviceGetAttribute(int* v, cudaDeviceAttr, int) { *v = 4; return cudaSuccess; }   // 4 emulated SMs
 inline cudaError_t cudaGetDeviceProperties(cudaDeviceProp* p, int) { *p = cudaDeviceProp{}; return cudaSuccess; }
 inline cudaError_t cudaSetDevice(int) { return cudaSuccess; }
 inline cudaError_t cudaGetDevice(int* d) { *d = 0; return cudaSuccess; }

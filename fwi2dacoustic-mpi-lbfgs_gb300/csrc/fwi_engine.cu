@@ -91,6 +91,7 @@ struct fwi_ctx {
     cudaEvent_t step_ev = nullptr, samp_ev[2]{}, samp_done = nullptr;
     bool samp_pending[2] = {false, false};         // a sample of that step parity is not yet waited for
     bool samp_used = false;                        // samp_st has work in this forward pass
+    int nsm = 1;                                   // streaming multiprocessors of the device
     cudaStream_t obs_st = nullptr;                 // fwi_gradient_obs: observed-trace upload under the forward phase
     cudaEvent_t obs_ev = nullptr;
     cudaGraph_t graph[3]{};        // captured phases (use_graph): forward, misfit, backward
@@ -328,6 +329,24 @@ const int* class_order(const fwi_ctx* x)
     return x->tune.class_order == 2 ? x_first : z_first;
 }
 
+// Grid of a general class of cnt tiles for n shots.  gen_grid 1: one block per
+// (tile, shot).  gen_grid k >= 2: k - 1 blocks per SM over the three classes,
+// split by the classes' work (tiles x the relative block time measured on C2:
+// z-general 1, x-general 1.3, corners 2.9), each block looping over its
+// class's items; the general work then keeps that many slots on every SM for
+// the whole step, beside the interior kernel, instead of running before it.
+dim3 gen_grid(const fwi_ctx* x, int cls, int cnt, int n)
+{
+    if (x->tune.gen_grid <= 1) return dim3(cnt, 1, n);
+    static const double cost[3] = {1.3, 1.0, 2.9};
+    double tot = 0.0;
+    for (int c = 0; c < 3; ++c) tot += cost[c] * (x->gen_off[c + 1] - x->gen_off[c]);
+    const double share = cost[cls] * cnt / tot;
+    const long long want = (long long)std::llround(share * (x->tune.gen_grid - 1) * x->nsm);
+    const long long items = (long long)cnt * n;
+    return dim3((unsigned)std::max(1LL, std::min(items, want)), 1, 1);
+}
+
 // Forks the side streams of the non-empty classes from st.
 void fork_classes(fwi_ctx* x)
 {
@@ -442,7 +461,9 @@ long long launch_fwd_step(fwi_ctx* x, StepParams& P, int lo, int hi, bool sample
         const int cnt = x->gen_off[cls + 1] - x->gen_off[cls];
         if (!cnt) continue;
         P.gen_tiles = x->gen_d + x->gen_off[cls];
-        const dim3 grid(cnt, 1, n);
+        P.gen_n = cnt;
+        P.gen_shots = n;
+        const dim3 grid = gen_grid(x, cls, cnt, n);
         cudaStream_t cs = class_stream(x, cls);
         if (x->tune.fwd_gen_blocks == 3) launch_fwd_gen<3>(cls, grid, block, cs, P);
         else launch_fwd_gen<4>(cls, grid, block, cs, P);
@@ -500,7 +521,9 @@ long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
         const int cnt = x->gen_off[cls + 1] - x->gen_off[cls];
         if (!cnt) continue;
         P.gen_tiles = x->gen_d + x->gen_off[cls];
-        const dim3 grid(cnt, 1, n);
+        P.gen_n = cnt;
+        P.gen_shots = n;
+        const dim3 grid = gen_grid(x, cls, cnt, n);
         cudaStream_t cs = class_stream(x, cls);
         if (x->tune.bwd_gen_blocks == 3) launch_bwd_edge<3>(cls, grid, block, cs, P);
         else launch_bwd_edge<4>(cls, grid, block, cs, P);
@@ -971,8 +994,10 @@ fwi_tuning default_tuning(const fwi_ctx* x)
     t.class_order = 1;
     t.serial = 2;
     t.priority = 1;
+    t.gen_grid = 1;
     return t;
 }
+
 
 // (Re)creates the general classes' side streams at the tuning's priority.
 cudaError_t make_side_streams(fwi_ctx* x)
@@ -1162,6 +1187,8 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
         return bail(FWI_ERR_NODEVICE);
     }
     if (cudaSetDevice(cfg->device) != cudaSuccess) return bail(FWI_ERR_NODEVICE);
+    if (cudaDeviceGetAttribute(&x->nsm, cudaDevAttrMultiProcessorCount, cfg->device) != cudaSuccess || x->nsm < 1)
+        return bail(FWI_ERR_CUDA);
     if (cudaStreamCreateWithFlags(&x->own, cudaStreamNonBlocking) != cudaSuccess) return bail(FWI_ERR_CUDA);
     x->st = x->own;
     for (auto& e : x->ev)
@@ -1751,7 +1778,7 @@ int fwi_set_stream(fwi_ctx* x, void* stream)
 int fwi_set_tuning(fwi_ctx* x, const fwi_tuning* t)
 {
     if (!x || !t) return FWI_ERR_ARG;
-    for (int i = 0; i < 7; ++i)
+    for (int i = 0; i < 6; ++i)
         if (t->reserved[i]) return fail(x, FWI_ERR_ARG, "fwi_tuning.reserved must be zero");
     const fwi_tuning d = default_tuning(x);
     fwi_tuning n = x->tune;
@@ -1765,6 +1792,7 @@ int fwi_set_tuning(fwi_ctx* x, const fwi_tuning* t)
     n.class_order = pick(t->class_order, d.class_order);
     n.serial = pick(t->serial, d.serial);
     n.priority = pick(t->priority, d.priority);
+    n.gen_grid = pick(t->gen_grid, d.gen_grid);
     const Geo& g = x->g;
     if (n.x_first < d.x_first || n.x_first % 4 || n.x_first >= g.pnx - g.npml - 4)
         return fail(x, FWI_ERR_ARG, "x_first must be a multiple of 4 from " + std::to_string(d.x_first));
@@ -1773,7 +1801,7 @@ int fwi_set_tuning(fwi_ctx* x, const fwi_tuning* t)
     if ((n.fwd_gen_blocks != 3 && n.fwd_gen_blocks != 4) || (n.bwd_gen_blocks != 3 && n.bwd_gen_blocks != 4) ||
         (n.fwd_int_blocks != 4 && n.fwd_int_blocks != 6) || (n.bwd_int_blocks != 3 && n.bwd_int_blocks != 4) ||
         (n.class_order != 1 && n.class_order != 2) || (n.serial != 1 && n.serial != 2) ||
-        (n.priority != 1 && n.priority != 2))
+        (n.priority != 1 && n.priority != 2) || n.gen_grid < 1 || n.gen_grid > 5)
         return fail(x, FWI_ERR_ARG, "a fwi_tuning value outside its list");
     CK(cudaSetDevice(x->cfg.device));
     CK(cudaStreamSynchronize(x->st));

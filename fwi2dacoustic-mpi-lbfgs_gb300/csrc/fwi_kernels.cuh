@@ -220,6 +220,8 @@ struct StepParams {
     int fast_tx0, fast_tz0;  // interior tile rectangle [fast_tx0, fast_tx1) x [fast_tz0, fast_tz1)
     int fast_tx1, fast_tz1;
     int gen_arith;           // general tiles follow from the rectangle (gen_tile_at), no list read
+    int gen_n;               // tiles of the general class launched
+    int gen_shots;           // shots of the launch (slots shot_base ..)
     const RecDev* recs;      // backward: receivers grouped by tile
     const int* rtile;        // backward: per-tile CSR of recs
     const float* wav;
@@ -756,19 +758,25 @@ __global__ void __launch_bounds__(NTH, MINB) k_fwd_gen(const StepParams P)
     __shared__ __align__(16) float su[TZ * UWP];
     __shared__ ZSiteTab tbz;
     __shared__ XSiteTab tbx;
-    const int s = blockIdx.z + P.shot_base;
-    const ShotDev sd = *GP(P.shots + s);
     const Geo& g = P.g;
-    const int2 t = P.gen_arith ? gen_tile_at(g, P.fast_tx0, P.fast_tx1, P.fast_tz0, P.fast_tz1, GX, GZ, blockIdx.x)
-                               : *GP(P.gen_tiles + blockIdx.x);
-    const int x0 = g.xoff + t.x * TX, z0 = g.zoff + t.y * TZ;
-    stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
-    // only active shots are launched; the test waits for nothing the copies need
-    if (P.step >= sd.nt) { cp_async_wait(); return; }
-    fill_sites<GX, GZ>(P, x0, z0, tbz, tbx);
-    cp_async_wait();
-    __syncthreads();
-    fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su, tbz, tbx);
+    // work items (tile, shot), item w = shot * gen_n + tile: one per block on a grid
+    // of gen_n x 1 x gen_shots blocks, or a loop over them on a smaller grid
+    const int nwork = P.gen_n * P.gen_shots, stride = gridDim.x * gridDim.z;
+    for (int w = blockIdx.z * gridDim.x + blockIdx.x; w < nwork; w += stride) {
+        if (w >= stride) __syncthreads();                  // the previous item's tables and tiles are read no more
+        const int gi = w % P.gen_n, s = P.shot_base + w / P.gen_n;
+        const ShotDev sd = *GP(P.shots + s);
+        const int2 t = P.gen_arith ? gen_tile_at(g, P.fast_tx0, P.fast_tx1, P.fast_tz0, P.fast_tz1, GX, GZ, gi)
+                                   : *GP(P.gen_tiles + gi);
+        const int x0 = g.xoff + t.x * TX, z0 = g.zoff + t.y * TZ;
+        stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
+        // only active shots are launched; the test waits for nothing the copies need
+        if (P.step >= sd.nt) { cp_async_wait(); continue; }
+        fill_sites<GX, GZ>(P, x0, z0, tbz, tbx);
+        cp_async_wait();
+        __syncthreads();
+        fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su, tbz, tbx);
+    }
 }
 
 // Forward step, interior tiles: no edge, CPML or strip cells, so every cell
@@ -1121,18 +1129,15 @@ __device__ __forceinline__ void adj_tile(const StepParams& P, const ShotDev& sd,
     }
 }
 
-// Backward step, tiles of the general path (edges, CPML, strips) of one
-// class (GX, GZ), from the list P.gen_tiles.
-template <bool GX, bool GZ, int MINB>
-__global__ void __launch_bounds__(NTH, MINB) k_bwd_edge(const StepParams P)
+// One general backward tile (edges, CPML, strips): general tile gi of the
+// class (GX, GZ), shot slot s.
+template <bool GX, bool GZ>
+__device__ __forceinline__ void bwd_edge_item(const StepParams& P, BwdSmem& sm, int gi, int s)
 {
-    FWI_DYN_SMEM(smraw);
-    BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
     const Geo& g = P.g;
-    const int2 t = P.gen_arith ? gen_tile_at(g, P.fast_tx0, P.fast_tx1, P.fast_tz0, P.fast_tz1, GX, GZ, blockIdx.x)
-                               : *GP(P.gen_tiles + blockIdx.x);
+    const int2 t = P.gen_arith ? gen_tile_at(g, P.fast_tx0, P.fast_tx1, P.fast_tz0, P.fast_tz1, GX, GZ, gi)
+                               : *GP(P.gen_tiles + gi);
     const int x0 = g.xoff + t.x * TX, z0 = g.zoff + t.y * TZ;
-    const int s = blockIdx.z + P.shot_base;
     const ShotDev sd = *GP(P.shots + s);
     const int m = P.step;
     const Coef& cf = P.c;
@@ -1245,6 +1250,21 @@ __global__ void __launch_bounds__(NTH, MINB) k_bwd_edge(const StepParams P)
             *GP(pold + o) = pn;
             *GP(gacc + o) = fmaf(bm[q * R + i], lp, gq[i]);
         }
+    }
+}
+
+// Backward step, the tiles of one general class (GX, GZ) from the list
+// P.gen_tiles (or gen_tile_at), for the launch's shots.
+template <bool GX, bool GZ, int MINB>
+__global__ void __launch_bounds__(NTH, MINB) k_bwd_edge(const StepParams P)
+{
+    FWI_DYN_SMEM(smraw);
+    BwdSmem& sm = *reinterpret_cast<BwdSmem*>(smraw);
+    // work items (tile, shot) as in k_fwd_gen
+    const int nwork = P.gen_n * P.gen_shots, stride = gridDim.x * gridDim.z;
+    for (int w = blockIdx.z * gridDim.x + blockIdx.x; w < nwork; w += stride) {
+        if (w >= stride) __syncthreads();                  // the previous item's shared memory is read no more
+        bwd_edge_item<GX, GZ>(P, sm, w % P.gen_n, P.shot_base + w / P.gen_n);
     }
 }
 

@@ -15,6 +15,10 @@ chosen at run time (include/fwi_gb300.h, ``fwi_tuning``):
   with the interior tiles and at which stream priority (``class_order``,
   ``serial``, ``priority``).
 
+``gen_grid`` (general classes on a fixed grid of blocks that loop over their
+tiles) is not swept: on C2 every setting was 7-57% slower per step than one
+block per tile, with and without the largest shared-memory carveout.
+
 ``autotune`` times a few forward and backward steps of the actual shot batch
 (``fwi_time_steps``, which replays them as CUDA graphs, as the gradient does)
 for each candidate, first the tile grid (coordinate by coordinate), then the

@@ -252,7 +252,12 @@ int fwi_get_stats(const fwi_ctx *ctx, fwi_stats *out);
  *       with the interior tiles;
  *   priority: 1 (default) gives the general classes' streams the same
  *       priority as the context's stream, 2 the device's highest, so that
- *       their (longer) blocks are scheduled first as SMs free up. */
+ *       their (longer) blocks are scheduled first as SMs free up;
+ *   gen_grid: 1 (default) launches one block per general tile and shot;
+ *       k = 2 .. 5 launches k - 1 blocks per SM over the general classes,
+ *       split by their work, each looping over its class's tiles, so that
+ *       the general work shares the SMs with the interior tiles for the
+ *       whole step instead of taking the device before them. */
 typedef struct fwi_tuning {
     int x_first, z_first;
     int fwd_gen_blocks, bwd_gen_blocks;
@@ -260,7 +265,8 @@ typedef struct fwi_tuning {
     int class_order;
     int serial;
     int priority;
-    int reserved[7];       /* zero */
+    int gen_grid;
+    int reserved[6];       /* zero */
 } fwi_tuning;
 /* FWI_ERR_ARG for a value outside the lists above. */
 int fwi_set_tuning(fwi_ctx *ctx, const fwi_tuning *tuning);

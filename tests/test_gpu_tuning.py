@@ -2,8 +2,8 @@
 
 * The kernel variants (register budgets for 3 or 4 general blocks per SM, 4
   or 6 interior forward blocks, 3 or 4 interior backward blocks), the class
-  order and serial launches run the same arithmetic per cell: the gradient is
-  bit-identical to the default's.
+  order, serial launches and the looping general grids (gen_grid) run the
+  same arithmetic per cell: the gradient is bit-identical to the default's.
 * Another tile grid (x_first / z_first) moves cells between the interior
   and the general kernels, whose x stencils differ in their rounding: the
   gradient stays within the parity tolerance of the FP64 oracle.
@@ -41,9 +41,10 @@ def test_kernel_variants_are_bit_identical(engine_lib, oracles):
     flat = np.concatenate([o.ravel() for o in case.oracle_obs(o64)])
     (J0, g0), t0 = _grad(case, flat)
     assert (t0["fwd_gen_blocks"], t0["bwd_gen_blocks"], t0["fwd_int_blocks"], t0["bwd_int_blocks"],
-            t0["class_order"], t0["serial"], t0["priority"]) == (4, 3, 6, 4, 1, 2, 1) and t0["x_first"] % 4 == 0
+            t0["class_order"], t0["serial"], t0["priority"], t0["gen_grid"]) == (4, 3, 6, 4, 1, 2, 1, 1)
+    assert t0["x_first"] % 4 == 0
     for tuning in ({"fwd_gen_blocks": 3, "bwd_gen_blocks": 4}, {"fwd_int_blocks": 4, "bwd_int_blocks": 3},
-                   {"class_order": 2}, {"serial": 1}, {"priority": 2}):
+                   {"class_order": 2}, {"serial": 1}, {"priority": 2}, {"gen_grid": 2}, {"gen_grid": 5}):
         (J, g), t = _grad(case, flat, tuning)
         assert all(t[k] == v for k, v in tuning.items())
         assert J == J0 and np.array_equal(g, g0), tuning
@@ -76,7 +77,7 @@ def test_tuning_rejects_bad_values(engine_lib, oracles):
     with case.engine() as e:
         t0 = e.tuning()
         for bad in ({"fwd_gen_blocks": 5}, {"fwd_int_blocks": 5}, {"bwd_int_blocks": 2}, {"class_order": 3},
-                    {"serial": 3}, {"priority": 3}, {"x_first": t0["x_first"] - 4},
+                    {"serial": 3}, {"priority": 3}, {"gen_grid": 6}, {"gen_grid": -1}, {"x_first": t0["x_first"] - 4},
                     {"x_first": t0["x_first"] + 2},
                     {"z_first": t0["z_first"] + 1}, {"x_first": 100000}):
             with pytest.raises(fwigpu.FwiError) as ei:
