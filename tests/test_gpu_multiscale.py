@@ -1,0 +1,169 @@
+"""Multiscale FWI with reduced-precision checkpoints, against the FP64 oracle.
+
+A reduced form of the 800 x 2400 precision-and-multiscale workload: the same
+pipeline on a 120 x 60 grid (free surface, 4 surface shots, nt 500):
+
+* three Butterworth low-pass bands (8, 12, 18 Hz, zero phase, order 6), applied
+  with fwi_bandpass (the reference's sfbandpass) to the source wavelet and to the
+  observed traces of every shot;
+* per band, 3 iterations of the device L-BFGS (MBotOpt's line search, FP64) on
+  the L2 misfit, the objective scaled once so that the first step moves the
+  model by about 10 m/s (small steps keep the line-search decisions away from
+  ties, so that runs whose gradients agree to rounding take the same path);
+* the gradient from the GPU with the strip ring (FP32), with FP16 checkpoints and
+  with BF16 checkpoints (absmax-scaled, 4 segments), and from the FP64 oracle.
+
+Checked: the misfit of every run falls in every band; each run's final model
+agrees with the oracle-driven run's, relative to that run's model update, to
+1e-3 for FP32 strips, 1.5e-2 for FP16 and 8e-2 for BF16 checkpoints (measured
+on a GB300: 4.6e-5, 5.4e-3 and 3.5e-2); the seismograms of the final model
+agree with the FP32 oracle to 2e-5; and one band inverted with the
+cross-correlation misfit (XCORR1D) lowers that misfit too.
+"""
+import numpy as np
+import pytest
+
+from test_gpu_parity import Case, rel
+
+pytestmark = pytest.mark.gpu
+
+NX, NZ, NPML, NT, DT, DX = 120, 60, 10, 500, 0.001, 10.0
+BANDS = (8.0, 12.0, 18.0)
+ITERS = 3
+
+
+def ricker(nt, dt, f0):
+    t = np.arange(nt) * dt - 1.2 / f0
+    a = (np.pi * f0 * t) ** 2
+    return ((1 - 2 * a) * np.exp(-a)).astype(np.float32)
+
+
+def smooth(v, r):
+    """Separable running mean of half width r (edge-replicated), twice."""
+    out = v.astype(np.float64)
+    for _ in range(2):
+        for ax in (0, 1):
+            pad = [(r, r) if a == ax else (0, 0) for a in (0, 1)]
+            p = np.pad(out, pad, mode="edge")
+            c = np.cumsum(p, axis=ax, dtype=np.float64)
+            c = np.concatenate([np.zeros_like(np.take(c, [0], axis=ax)), c], axis=ax)
+            n = out.shape[ax]
+            out = (np.take(c, np.arange(2 * r + 1, 2 * r + 1 + n), axis=ax) - np.take(c, np.arange(n), axis=ax)) / (2 * r + 1)
+    return out.astype(np.float32)
+
+
+def models():
+    z = np.arange(NZ)[:, None] * DX
+    x = np.arange(NX)[None, :] * DX
+    vtrue = (1800.0 + 1.6 * z + 0 * x).astype(np.float32)
+    vtrue += (250.0 * np.exp(-((z - 300) ** 2 + (x - 500) ** 2) / (2 * 60.0 ** 2))).astype(np.float32)
+    vtrue -= (200.0 * np.exp(-((z - 380) ** 2 + (x - 850) ** 2) / (2 * 50.0 ** 2))).astype(np.float32)
+    return vtrue, smooth(vtrue, 8)
+
+
+def band_case(O, wav):
+    irx = np.arange(2, NX - 2, 2)
+    shots = [(isx, 1, irx, np.ones_like(irx), wav) for isx in (15, 45, 75, 105)]
+    return Case(O, 1, nx=NX, nz=NZ, npml=NPML, nt=NT, jump=1, dx=DX, dz=DX, dt=DT, shots=shots)
+
+
+def invert(x0, evaluate, scale):
+    import fwigpu
+    x = x0.astype(np.float64).ravel().copy()
+    f, g = evaluate(x)
+    f0 = f
+    opt = fwigpu.Lbfgs(x.size, max_iterations=ITERS)
+    state = opt.begin(x, scale * f, scale * g)
+    n = 0
+    while state == fwigpu.LBFGS_EVALUATE and n < 40:
+        f, g = evaluate(x)
+        state = opt.next(x, scale * f, scale * g)
+        n += 1
+    opt.close()
+    f, _ = evaluate(x)
+    return x.reshape(x0.shape).astype(np.float32), f0, f
+
+
+def test_multiscale_inversion_with_checkpoints(engine_lib, oracles):
+    import fwigpu
+    O, o32, o64 = oracles
+    vtrue, vstart = models()
+    w = ricker(NT, DT, 15.0)
+    base = band_case(O, w)
+    obs_full = [o64.forward(base.oracle_cfg_for(NT), vtrue, s).astype(np.float32) for s in base.oshots]
+    bands = []
+    for fb in BANDS:
+        wb = fwigpu.bandpass(w[None, :], DT, 0, 6, 6, fb, 0.0)[0]
+        ob = [fwigpu.bandpass(o, DT, 0, 6, 6, fb, 0.0) for o in obs_full]
+        bands.append((band_case(O, wb), ob))
+
+    def oracle_eval(case, obs):
+        def ev(xv):
+            v = xv.reshape(vstart.shape).astype(np.float32)
+            J, g = 0.0, None
+            for s, ob in zip(case.oshots, obs):
+                j, gg, _ = o64.gradient(case.oracle_cfg_for(NT), v, [s], [ob])
+                J += j
+                g = gg if g is None else g + gg
+            return J, g.ravel()
+        return ev
+
+    # one objective scale for every run: from the oracle gradient of the first band
+    _, g0 = oracle_eval(*bands[0])(vstart.ravel())
+    scale = 10.0 / np.abs(g0).max()
+
+    def run(make_eval):
+        x = vstart.copy()
+        for case, obs in bands:
+            x, f0, f1 = invert(x, make_eval(case, obs), scale)
+            assert f1 < f0, (f0, f1)
+        return x
+
+    final = {"oracle": run(oracle_eval)}
+    c = base.ecfg
+    variants = {"strips": {}, "f16": dict(store=fwigpu.STORE_SNAPSHOTS, snapshots=4, snap_precision="f16"),
+                "bf16": dict(store=fwigpu.STORE_SNAPSHOTS, snapshots=4, snap_precision="bf16")}
+    for name, kw in variants.items():
+        cfg = fwigpu.make_config(c.nx, c.nz, c.dx, c.dz, c.dt, c.nt_max, npml=c.npml, free_surface=1, jump=1, **kw)
+        with fwigpu.Engine(cfg) as e:
+            def gpu_eval(case, obs):
+                e.set_shots(case.eshots)
+                e.set_observed(np.concatenate([o.ravel() for o in obs]))
+
+                def ev(xv):
+                    e.set_model(xv.reshape(vstart.shape).astype(np.float32))
+                    J, g = e.gradient()
+                    return J, g.ravel()
+                return ev
+            final[name] = run(gpu_eval)
+            if name == "strips":
+                # seismograms of the final model against the FP32 oracle
+                e.set_shots(base.eshots)
+                e.set_model(final[name])
+                syn = e.split(e.forward())
+                for s, got in zip(base.oshots, syn):
+                    assert rel(got, o32.forward(base.oracle_cfg_for(NT), final[name], s)) <= 2e-5
+    upd = final["oracle"].astype(np.float64) - vstart
+    assert np.linalg.norm(upd) > 1.0                     # the inversion moved the model
+    errs = {name: float(np.linalg.norm(final[name].astype(np.float64) - final["oracle"]) / np.linalg.norm(upd))
+            for name in ("strips", "f16", "bf16")}
+    print("final-model error against the oracle-driven run:", errs)
+    for name, tol in (("strips", 1e-3), ("f16", 1.5e-2), ("bf16", 8e-2)):
+        assert errs[name] <= tol, errs
+    for name, x in final.items():
+        assert np.isfinite(x).all() and x.min() > 1000.0, name
+
+    # one band with the cross-correlation misfit (XCORR1D, middle slice)
+    case, obs = bands[1]
+    with fwigpu.Engine(base.ecfg) as e:
+        e.set_shots(case.eshots)
+        e.set_observed(np.concatenate([o.ravel() for o in obs]))
+        e.set_misfit(fwigpu.MISFIT_XCORR)
+
+        def ev(xv):
+            e.set_model(xv.reshape(vstart.shape).astype(np.float32))
+            J, g = e.gradient()
+            return J, g.ravel()
+        _, gx = ev(vstart.ravel())
+        _, f0, f1 = invert(vstart, ev, 10.0 / np.abs(gx).max())
+        assert f1 < f0, (f0, f1)
