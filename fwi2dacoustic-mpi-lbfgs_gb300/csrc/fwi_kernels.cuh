@@ -628,6 +628,12 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
         const bool gxc = GX && x_window_general(g, x0 + BX * h, BX);        // this half needs the x-general formulas
         const int cl = tx + BX * h, c = x0 + cl;
         const bool cin = !GX || (c >= 0 && c < g.pnx);                      // z sites exist in grid columns only
+        // strip cells (saved for the backward rebuild) of this unit: its rows meet the
+        // first or last NSTRIP physical rows, or this column is one of the first or last
+        // NSTRIP physical columns; save_strip checks each cell again
+        const int izu = r0 - g.z0p, ixc = c - g.x0p;
+        const bool strip_rows = gzw && ((izu < NSTRIP && izu + R > 0) || (izu + R > g.nz - NSTRIP && izu < g.nz));
+        const bool strip_col = gxc && ((ixc >= 0 && ixc < NSTRIP) || (ixc >= g.nx - NSTRIP && ixc < g.nx));
         // every global operand of this column segment first: K, p^{it-1} and the psi entries
         float kq[R], po[R], pvv[R + 3], pux[R], pvz[R];
         const int xoff = gxc ? tbx.xux[cl + 3].off : -1;                     // the ux site of column c
@@ -740,7 +746,7 @@ __device__ __forceinline__ void fwd_tile(const StepParams& P, const ShotDev& sd,
                 float pn = fmaf(kq[i], ux + vz, fmaf(2.f, pc[i + 3], -po[i]));      // fwi_2d.c:878
                 if (row == sd.src_r && c == sd.src_c) pn += amp * kq[i];
                 *GP(pold + o) = pn;
-                if (gzw || gxc) save_strip(P, sd, row, c, pn, P.step);    // plain windows hold no strip cell
+                if (strip_rows || strip_col) save_strip(P, sd, row, c, pn, P.step);
             }
         }
     }
