@@ -4,8 +4,8 @@ Tolerances (FP32 stencils on both sides; the GPU contracts a*b+c into FMA,
 the oracle does not, so results agree to rounding, not bit for bit):
   * seismograms vs the FP32 oracle: relative L2 error <= 2e-5 per shot;
   * misfit vs the FP64 oracle: relative error <= 1e-5;
-  * gradient vs the FP64 oracle: relative L2 error <= 1e-4 (the benchmark spec's
-    bound), and vs the FP32 oracle the same bound.
+  * gradient vs the FP64 oracle: relative L2 error <= 1e-4 (the project's
+    FP32 gradient tolerance), and vs the FP32 oracle the same bound.
 """
 import numpy as np
 import pytest

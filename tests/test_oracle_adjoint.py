@@ -8,7 +8,7 @@ tests are its only pin):
 * adjoint of the whole time stepping: <F w, r> == <w, F^T r> where F maps the
   source wavelet to the seismogram;
 * central finite differences of the L2 misfit along random perturbations;
-* FP32 twin against FP64 twin (the benchmark spec's <= 1e-4 relative error).
+* FP32 twin against FP64 twin (<= 1e-4 relative error, the FP32 gradient tolerance).
 """
 import numpy as np
 import pytest
@@ -92,7 +92,7 @@ def test_gradient_finite_differences(oracles, fs, order):
         an = (g * (vp.astype(np.float64) - vm)).sum()
         # limited by the FP32 rounding of K = v^2 dt^2 (about 6e-8 relative)
         assert abs(fd - an) <= 5e-4 * abs(an), (eps, fd, an)
-    # the FP32 twin stays within the benchmark spec's 1e-4 of the FP64 twin
+    # the FP32 twin stays within 1e-4 (the FP32 gradient tolerance) of the FP64 twin
     J32, g32, _ = o32.gradient(cfg, vel, [sh], [obs])
     assert abs(J32 - J0) <= 1e-5 * J0
     assert np.linalg.norm(g32 - g) <= 1e-4 * np.linalg.norm(g)
