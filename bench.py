@@ -290,7 +290,8 @@ def run_reference(args):
 
 
 def aux_leg(local):
-    """The routines around the gradient on C2-sized data, each through the C
+    """The routines around the gradient on data of the 560 x 1700, 64-shot
+    workload's sizes, each through the C
     ABI (host buffers in and out, device buffers allocated per call) against
     the reference's own compiled routine on one host core (the reference runs
     them serially): sfbandpass on one shot record of 1700 traces x 4000
@@ -600,7 +601,7 @@ def run_ours(args):
             J_s, g_s = se.gradient()
         line["vs_strips"] = {"grad_rel_diff": float(np.linalg.norm(g_c - g_s) / np.linalg.norm(g_s)),
                              "misfit_equal": bool(J_c == J_s),
-                             "note": "the strip ring's gradient is within 5e-6 of the FP64 oracle on C2"}
+                             "note": "the strip ring's gradient is within 5e-6 of the FP64 oracle on the 560 x 1700 workload"}
 
     # CPU baseline (the reference's own kernels, or their restatement) and the accuracy check
     if "cpu" not in skip and rank == 0 and world == 1:

@@ -322,7 +322,8 @@ bool sample_aside(const fwi_ctx* x) { return concurrent(x); }
 
 // Launch order of the general classes (0 = x-general, 1 = z-general, 2 =
 // corners).  By default the z-general blocks, the most numerous and longest,
-// start first (2.5% shorter forward steps than x, z, corners on C2).
+// start first (2.5% shorter forward steps than x, z, corners on the 560 x 1700,
+// 64-shot workload).
 const int* class_order(const fwi_ctx* x)
 {
     static const int z_first[3] = {1, 0, 2}, x_first[3] = {0, 1, 2};
@@ -331,7 +332,7 @@ const int* class_order(const fwi_ctx* x)
 
 // Grid of a general class of cnt tiles for n shots.  gen_grid 1: one block per
 // (tile, shot).  gen_grid k >= 2: k - 1 blocks per SM over the three classes,
-// split by the classes' work (tiles x the relative block time measured on C2:
+// split by the classes' work (tiles x the relative block time measured on the 560 x 1700, 64-shot workload:
 // z-general 1, x-general 1.3, corners 2.9), each block looping over its
 // class's items; the general work then keeps that many slots on every SM for
 // the whole step, beside the interior kernel, instead of running before it.

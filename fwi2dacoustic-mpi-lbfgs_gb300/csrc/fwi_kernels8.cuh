@@ -16,8 +16,8 @@
 //
 // The kernels run in passes over the whole padded grid of every active shot
 // (grid.z = shot slot), with the staggered quantities in HBM buffers of the
-// field layout: the 8th-order path serves the small configurations (C1:
-// 221 x 441 padded cells, whose whole state stays in the 129 MB L2), where a
+// field layout: the 8th-order path serves small grids (the 201 x 401, 8-shot
+// workload: 221 x 441 padded cells, whose whole state stays in the 129 MB L2), where a
 // fused tile kernel would not pay for its halo of 7 cells.  Per step:
 //   forward:  k8_uv (u, v with their psi), k8_fwd (ux, vz with psi,
 //             leapfrog, source, strips), then the shared receiver sampling;

@@ -16,7 +16,8 @@ chosen at run time (include/fwi_gb300.h, ``fwi_tuning``):
   ``serial``, ``priority``).
 
 ``gen_grid`` (general classes on a fixed grid of blocks that loop over their
-tiles) is not swept: on C2 every setting was 7-57% slower per step than one
+tiles) is not swept: on the 560 x 1700, 64-shot workload every setting was
+7-57% slower per step than one
 block per tile, with and without the largest shared-memory carveout.
 
 ``autotune`` times a few forward and backward steps of the actual shot batch

@@ -1,7 +1,8 @@
 """GPU parity of the routines around the gradient (tests/aux_cases.py):
 gradient preconditioning and Butterworth band-pass bit-identical to the
 oracle (and so to the reference), XCORR1D and the XCORR gradient within
-tolerance, at test sizes and at the C2 grid / trace sizes."""
+tolerance, at test sizes and at the grid / trace sizes of the 560 x 1700,
+4000-step workload."""
 import numpy as np
 import pytest
 
@@ -32,7 +33,8 @@ def test_xcorr1d(aux):
 
 
 def test_xcorr_long_traces(aux):
-    """C2-length traces (nt0 = 2001), both slices, against the oracle."""
+    """Traces as long as the 560 x 1700 workload's (nt0 = 2001), both slices,
+    against the oracle."""
     import fwigpu
     rng = np.random.default_rng(23)
     nr, nt = 12, 2001

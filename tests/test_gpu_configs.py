@@ -1,12 +1,12 @@
 """GPU parity at the benchmark configurations' sizes and shapes.
 
-* C1 at full size: 201 x 401 grid, dx 10 m, dt 1 ms, nt 2000, CPML 20,
+* The 8th-order inversion workload at full size: 201 x 401 grid, dx 10 m, dt 1 ms, nt 2000, CPML 20,
   8 surface shots, 10 Hz Ricker, 200 receivers at 2 m depth, the layered
   model with 3 Gaussian anomalies and its triangle-smoothed start model.
   Seismograms of every shot against the FP32 oracle (relative L2 <= 2e-5),
   the whole 8-shot gradient against the FP64 oracle (<= 1e-4) and the misfit
   (<= 1e-5).
-* C3 at a quarter of its size: 150 x 500 grid, 64 shots with uneven records
+* The uneven 256-shot batch (600 x 2000) at a quarter of its size: 150 x 500 grid, 64 shots with uneven records
   (750-1500 steps, sorted into the active-prefix launches, several shots
   ending mid-loop) and uneven off-end spreads.  Gradient against the FP64
   oracle (<= 1e-4), and the batched gradient against the plain per-shot path

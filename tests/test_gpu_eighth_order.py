@@ -3,8 +3,8 @@ CPU oracle, whose operator and adjoint are pinned by tests/test_oracle_adjoint.p
 (the reference has no 8th-order code to pin against).
 
 Tolerances as for the reference's 4th order: seismograms vs the FP32 oracle
-<= 2e-5, misfit vs FP64 <= 1e-5, gradient vs FP64 <= 1e-4.  C1 runs as
-configured: 201 x 401, nt 2000, 8 shots, 200 receivers, 8th order, one
+<= 2e-5, misfit vs FP64 <= 1e-5, gradient vs FP64 <= 1e-4.  The 8th-order
+inversion workload runs as configured: 201 x 401, nt 2000, 8 shots, 200 receivers, 8th order, one
 gradient checked against the FP64 oracle, then 5 L-BFGS iterations on the
 device (fwi_lbfgs_*) driven by the engine's gradients.
 """
