@@ -15,8 +15,9 @@ small grid with the reference's operators, for each perturbation dv:
 * the GPU gradient g (FP32 stencils, FP64 shot reduction) gives
   an = <g, v+ - v-> at e = EPS, the same first-order change.
 
-Both the strip-ring gradient and the checkpointed one (FP32 checkpoints of
-the forward state, 5 segments) must match every finite difference to
+With a free surface and with CPML on all sides, both the strip-ring gradient
+and the checkpointed one (FP32 checkpoints of the forward state, 5 segments)
+must match every finite difference to
 2e-3 relative, plus a floor of 2e-5 |g| |v+ - v-| for directions that are
 nearly orthogonal to g.  The median relative error must stay below 5e-4,
 the bound the FP64 oracle's own finite-difference test uses: the discrete
@@ -53,10 +54,11 @@ def misfit64(o64, case, vel, obs):
     return J
 
 
-def test_gradient_against_central_finite_differences(engine_lib, oracles):
+@pytest.mark.parametrize("fs", [1, 0])
+def test_gradient_against_central_finite_differences(engine_lib, oracles, fs):
     import fwigpu
     O, _, o64 = oracles
-    case = Case(O, 1, seed=91, nt=201)
+    case = Case(O, fs, seed=91 + fs, nt=201)
     obs = case.oracle_obs(o64)
     flat = np.concatenate([o.ravel() for o in obs])
     grads = {}
@@ -74,7 +76,7 @@ def test_gradient_against_central_finite_differences(engine_lib, oracles):
     for J, _ in grads.values():
         assert abs(J - J0) <= 1e-4 * J0, (J, J0)      # FP32 fields: 1.4e-5 on this short record
 
-    rng = np.random.default_rng(2024)
+    rng = np.random.default_rng(2024 + fs)
     nz, nx = case.vel.shape
     errs = {name: [] for name in grads}
     for _ in range(NPERT):
