@@ -40,35 +40,40 @@ def stale() -> bool:
     return any(os.path.getmtime(d) > t for d in DEPS)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compiles the three translation units in parallel, then links them."""
-    if not force and not stale():
+def build(force: bool = False, verbose: bool = False, defines=(), out: str | None = None) -> str:
+    """Compiles the three translation units in parallel, then links them.
+
+    defines (e.g. ("FWI_TIMELINE",)) and out build a diagnostics variant into
+    its own library and object directory; the product library is LIB."""
+    lib = out or LIB
+    if not force and not defines and not stale():
         return LIB
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     flags = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
+    flags += ["-D" + d for d in defines]
     # FWI_NVCC_EXTRA adds diagnostics flags, e.g. -DFWI_SELF_CHECK
     flags = os.environ.get("FWI_NVCC_EXTRA", "").split() + flags
     if verbose:
         flags.append("-Xptxas=-v")
-    objdir = os.path.join(PKG, "_build")
+    objdir = os.path.join(PKG, "_build", *(["variant_" + "_".join(d.lower() for d in defines)] if defines else []))
     os.makedirs(objdir, exist_ok=True)
     objs = [os.path.join(objdir, os.path.basename(src)[:-3] + ".o") for src in SOURCES]
     procs = [subprocess.Popen([nvcc()] + flags + ["-c", src, "-o", obj], stdout=subprocess.PIPE,
                               stderr=subprocess.PIPE, text=True) for src, obj in zip(SOURCES, objs)]
     errors = ""
     for p in procs:
-        out, err = p.communicate()
+        so, se = p.communicate()
         if verbose:
-            sys.stderr.write(err)
+            sys.stderr.write(se)
         if p.returncode != 0:
-            errors += out + err
+            errors += so + se
     if errors:
         raise RuntimeError("nvcc failed:\n" + errors)
     r = subprocess.run([nvcc(), ARCH, "-shared", "-o", tmp] + objs, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc link failed:\n" + r.stdout + r.stderr)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 EMU_LIB = os.path.join(PKG, "libfwiemu.so")

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <mutex>
 #include <cstdio>
 #include <cstring>
@@ -92,6 +93,10 @@ struct fwi_ctx {
     bool samp_pending[2] = {false, false};         // a sample of that step parity is not yet waited for
     bool samp_used = false;                        // samp_st has work in this forward pass
     int nsm = 1;                                   // streaming multiprocessors of the device
+#ifdef FWI_TIMELINE
+    unsigned long long* tl_d = nullptr;            // block timeline (diagnostics build), written out on destroy
+    std::string tl_out;
+#endif
     cudaStream_t obs_st = nullptr;                 // fwi_gradient_obs: observed-trace upload under the forward phase
     cudaEvent_t obs_ev = nullptr;
     cudaGraph_t graph[3]{};        // captured phases (use_graph): forward, misfit, backward
@@ -1195,6 +1200,18 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
     for (auto& e : x->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return bail(FWI_ERR_CUDA);
     x->tune = default_tuning(x);
+#ifdef FWI_TIMELINE
+    if (const char* st = std::getenv("FWI_TIMELINE_STEP")) {
+        const char* out = std::getenv("FWI_TIMELINE_OUT");
+        x->tl_out = out ? out : "timeline.bin";
+        const size_t bytes = sizeof(unsigned long long) * 8 * TL_ITEMS * 2;
+        const int step = std::atoi(st);
+        if (cudaMalloc(&x->tl_d, bytes) != cudaSuccess || cudaMemset(x->tl_d, 0, bytes) != cudaSuccess ||
+            cudaMemcpyToSymbol(g_tl, &x->tl_d, sizeof(x->tl_d)) != cudaSuccess ||
+            cudaMemcpyToSymbol(g_tl_step, &step, sizeof(int)) != cudaSuccess)
+            return bail(FWI_ERR_CUDA);
+    }
+#endif
     if (make_side_streams(x) != cudaSuccess) return bail(FWI_ERR_CUDA);
     for (int i = 0; i < 3; ++i)
         if (cudaEventCreateWithFlags(&x->join_ev[i], cudaEventDisableTiming) != cudaSuccess) return bail(FWI_ERR_CUDA);
@@ -1271,6 +1288,20 @@ fwi_ctx* fwi_create(const fwi_config* cfg, int* status)
 void fwi_destroy(fwi_ctx* x)
 {
     if (!x) return;
+#ifdef FWI_TIMELINE
+    if (x->tl_d) {
+        std::vector<unsigned long long> h((size_t)8 * TL_ITEMS * 2);
+        if (cudaMemcpy(h.data(), x->tl_d, h.size() * sizeof(h[0]), cudaMemcpyDeviceToHost) == cudaSuccess) {
+            if (FILE* f = std::fopen(x->tl_out.c_str(), "wb")) {
+                std::fwrite(h.data(), sizeof(h[0]), h.size(), f);
+                std::fclose(f);
+            }
+        }
+        unsigned long long* none = nullptr;
+        cudaMemcpyToSymbol(g_tl, &none, sizeof(none));
+        cudaFree(x->tl_d);
+    }
+#endif
     free_shots(x);
     void* ps[] = {x->K, x->vel, x->pmlc, x->grad, x->gradf, x->gen_d, x->err_d};
     for (void* p : ps) if (p) cudaFree(p);

@@ -95,6 +95,35 @@ __device__ inline T* gptr(T* p, int site)
 #define GP(p) (p)
 #endif
 
+// Block timeline diagnostics build (FWI_TIMELINE, never the product build):
+// thread (0, 0) of every block of the stencil kernels records %globaltimer
+// when the block starts a work item and, after a barrier, when it ends it,
+// at one time step (g_tl_step), into g_tl[class][item][start, end].  Classes:
+// 0 interior backward, 1 z-general, 2 x-general, 3 corner backward tiles,
+// 4 interior forward, 5-7 the forward general classes.  The engine arms it
+// from the environment (FWI_TIMELINE_STEP, FWI_TIMELINE_OUT) and writes the
+// buffer out when the context is destroyed; the product build compiles
+// FWI_TL to nothing.
+constexpr long long TL_ITEMS = 1LL << 16;        // items recorded per class
+#ifdef FWI_TIMELINE
+__device__ unsigned long long* g_tl = nullptr;
+__device__ int g_tl_step = -1;
+__device__ __forceinline__ void tl_stamp(int step, int cls, long long item, int end)
+{
+    if (!g_tl || step != g_tl_step || threadIdx.x != 0 || threadIdx.y != 0 || item < 0 || item >= TL_ITEMS) return;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    g_tl[((long long)cls * TL_ITEMS + item) * 2 + end] = t;
+}
+#define FWI_TL(step, cls, item, end) tl_stamp((step), (cls), (item), (end))
+#define FWI_TL_END(step, cls, item) do { __syncthreads(); tl_stamp((step), (cls), (item), 1); } while (0)
+#else
+#define FWI_TL(step, cls, item, end) ((void)0)
+#define FWI_TL_END(step, cls, item) ((void)0)
+#endif
+// Timeline class of a general tile class (GX, GZ): base + 1 z-general, + 2 x-general, + 3 corners.
+__host__ __device__ constexpr int tl_class(bool gx, bool gz, int base) { return base + (gx && gz ? 3 : gx ? 2 : 1); }
+
 constexpr int TX = 64;             // tile width  (cells)
 constexpr int TZ = 32;             // tile height (cells)
 constexpr int BX = 32;             // threads in x
@@ -771,6 +800,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_fwd_gen(const StepParams P)
     for (int w = blockIdx.z * gridDim.x + blockIdx.x; w < nwork; w += stride) {
         if (w >= stride) __syncthreads();                  // the previous item's tables and tiles are read no more
         const int gi = w % P.gen_n, s = P.shot_base + w / P.gen_n;
+        FWI_TL(P.step, tl_class(GX, GZ, 4), w, 0);
         const ShotDev sd = *GP(P.shots + s);
         const int2 t = P.gen_arith ? gen_tile_at(g, P.fast_tx0, P.fast_tx1, P.fast_tz0, P.fast_tz1, GX, GZ, gi)
                                    : *GP(P.gen_tiles + gi);
@@ -782,6 +812,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_fwd_gen(const StepParams P)
         cp_async_wait();
         __syncthreads();
         fwd_tile<GX, GZ>(P, sd, s, x0, z0, sp, su, tbz, tbx);
+        FWI_TL_END(P.step, tl_class(GX, GZ, 4), w);
     }
 }
 
@@ -802,6 +833,8 @@ __global__ void __launch_bounds__(NTH, MINB) k_fwd_fast(const __grid_constant__ 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const long long so = (long long)s * g.fstride;
     const int r0l = R * ty, r0 = z0 + r0l;
+    [[maybe_unused]] const long long tl_item = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    FWI_TL(P.step, 4, tl_item, 0);
     // this thread's cells: rows r0 + i, columns x0 + tx + BX h, at 32-bit offsets i ld + BX h
     const long long o0 = (long long)r0 * g.ld + x0 + tx;
     float* __restrict__ prow = P.pold + so + o0;
@@ -853,6 +886,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_fwd_fast(const __grid_constant__ 
             __stcg(GP(prow + i * g.ld + BX * h), pn);
         }
     }
+    FWI_TL_END(P.step, 4, tl_item);
 }
 
 // syn[r][it/jump] = p^{it+1}(receiver r) for every receiver of the launched shots.
@@ -1270,7 +1304,9 @@ __global__ void __launch_bounds__(NTH, MINB) k_bwd_edge(const StepParams P)
     const int nwork = P.gen_n * P.gen_shots, stride = gridDim.x * gridDim.z;
     for (int w = blockIdx.z * gridDim.x + blockIdx.x; w < nwork; w += stride) {
         if (w >= stride) __syncthreads();                  // the previous item's shared memory is read no more
+        FWI_TL(P.step, tl_class(GX, GZ, 0), w, 0);
         bwd_edge_item<GX, GZ>(P, sm, w % P.gen_n, P.shot_base + w / P.gen_n);
+        FWI_TL_END(P.step, tl_class(GX, GZ, 0), w);
     }
 }
 
@@ -1323,6 +1359,8 @@ __global__ void __launch_bounds__(NTH, MINB) k_bwd_int(const __grid_constant__ S
     float* __restrict__ gacc = P.gacc + so;
     const int r0l = R * ty, r0 = z0 + r0l;
     [[maybe_unused]] constexpr int NS = SPH * SPW;
+    [[maybe_unused]] const long long tl_item = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    FWI_TL(P.step, 0, tl_item, 0);
 
 #ifndef FWI_CPU_EMU
     if (tid == 0) mbar_init(&sm.bar);
@@ -1423,6 +1461,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_bwd_int(const __grid_constant__ S
             __stcg(GP(gacc + o), fmaf(bm[q], lp, ga[q]));
         }
     }
+    FWI_TL_END(P.step, 0, tl_item);
 }
 
 // ---------------------------------------------------------------------------
