@@ -302,6 +302,16 @@ __host__ __device__ inline bool tile_z_general(const Geo& g, int z0) { return z_
 // and pnz-2, and the free-surface terms of rows up to 4), which is the wider.
 __device__ __forceinline__ bool z_unit_edge(const Geo& g, int r0) { return r0 < 8 || r0 + R + 4 > g.pnz; }
 
+// Staged rows a z-only general tile reads: those of its rows inside the padded
+// grid and HZ more on either side (staged row r holds grid row z0 - HZ + r).
+// Its row-group units start inside the grid and every cell it writes reads
+// rows within HZ of its own, so the rows outside this range (most of a tile
+// above the first grid row) need not be copied.
+__device__ __forceinline__ int2 z_tile_rows(const Geo& g, int z0)
+{
+    return make_int2(max(z0, 0) - z0, min(z0 + TZ, g.pnz) - z0 + 2 * HZ);
+}
+
 // Tile i of a general class, from the interior tile rectangle [tx0, tx1) x
 // [tz0, tz1): the x-general class is the general columns (left, then right)
 // of the interior rows, the z-general class the interior columns of the
@@ -514,11 +524,13 @@ __device__ __forceinline__ bool tma_wait(unsigned long long* bar, int* err)
 // Starts copying the (TZ+2HZ) x (TX+2HX) tile of field f whose interior
 // starts at (z0, x0) into shared memory in 16-byte pieces; cp_async_wait()
 // and a barrier must follow before the tile is read.
-__device__ __forceinline__ void stage_tile(const float* __restrict__ f, const Geo& g, int x0, int z0, float* sp)
+// Rows r_lo .. r_hi - 1 of the staged tile only (default: all SPH rows).
+__device__ __forceinline__ void stage_tile(const float* __restrict__ f, const Geo& g, int x0, int z0, float* sp,
+                                           int r_lo = 0, int r_hi = SPH)
 {
     const int tid = threadIdx.y * BX + threadIdx.x;
     constexpr int Q = SPW / 4;
-    for (int i = tid; i < SPH * Q; i += NTH) {
+    for (int i = r_lo * Q + tid; i < r_hi * Q; i += NTH) {
         const int r = i / Q, q = i - r * Q;
         const float4* src = reinterpret_cast<const float4*>(f + (long long)(z0 - HZ + r) * g.ld + (x0 - HX) + 4 * q);
         cp_async16(sp + SIDX(r * SPW + 4 * q, SPH * SPW), GP(src));
@@ -805,7 +817,8 @@ __global__ void __launch_bounds__(NTH, MINB) k_fwd_gen(const StepParams P)
         const int2 t = P.gen_arith ? gen_tile_at(g, P.fast_tx0, P.fast_tx1, P.fast_tz0, P.fast_tz1, GX, GZ, gi)
                                    : *GP(P.gen_tiles + gi);
         const int x0 = g.xoff + t.x * TX, z0 = g.zoff + t.y * TZ;
-        stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp);
+        const int2 zr = (GZ && !GX) ? z_tile_rows(g, z0) : make_int2(0, SPH);
+        stage_tile(P.pcur + (long long)s * g.fstride, g, x0, z0, sp, zr.x, zr.y);
         // only active shots are launched; the test waits for nothing the copies need
         if (P.step >= sd.nt) { cp_async_wait(); continue; }
         fill_sites<GX, GZ>(P, x0, z0, tbz, tbx);
@@ -1190,8 +1203,9 @@ __device__ __forceinline__ void bwd_edge_item(const StepParams& P, BwdSmem& sm, 
     const int zp0 = g.z0p, zp1 = g.z0p + g.nz, xp0 = g.x0p, xp1 = g.x0p + g.nx;
     const bool phys = z0 < zp1 && z0 + TZ > zp0 && x0 < xp1 && x0 + TX > xp0;
 
-    stage_tile(P.bcur + so, g, x0, z0, sm.sq);
-    if (phys) stage_tile(P.pcur + so, g, x0, z0, sm.sp);
+    const int2 zr = (GZ && !GX) ? z_tile_rows(g, z0) : make_int2(0, SPH);
+    stage_tile(P.bcur + so, g, x0, z0, sm.sq, zr.x, zr.y);
+    if (phys) stage_tile(P.pcur + so, g, x0, z0, sm.sp, zr.x, zr.y);
     // only active shots are launched; the test comes after the copies are issued
     if (m > sd.nt) { cp_async_wait(); return; }
 
