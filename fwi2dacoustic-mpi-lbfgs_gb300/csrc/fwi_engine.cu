@@ -337,10 +337,11 @@ const int* class_order(const fwi_ctx* x)
 
 // Grid of a general class of cnt tiles for n shots.  gen_grid 1: one block per
 // (tile, shot).  gen_grid k >= 2: k - 1 blocks per SM over the three classes,
-// split by the classes' work (tiles x the relative block time measured on the 560 x 1700, 64-shot workload:
-// z-general 1, x-general 1.3, corners 2.9), each block looping over its
-// class's items; the general work then keeps that many slots on every SM for
-// the whole step, beside the interior kernel, instead of running before it.
+// split by the classes' work (tiles x the relative block time measured on the
+// 560 x 1700, 64-shot workload: z-general 1, x-general 1.3, corners 2.9), each
+// block looping over its class's items, so that the general work would keep
+// that many slots on every SM for the whole step instead of running before the
+// interior tiles.  Measured slower than gen_grid 1 at every k.
 dim3 gen_grid(const fwi_ctx* x, int cls, int cnt, int n)
 {
     if (x->tune.gen_grid <= 1) return dim3(cnt, 1, n);
@@ -1003,7 +1004,6 @@ fwi_tuning default_tuning(const fwi_ctx* x)
     t.gen_grid = 1;
     return t;
 }
-
 
 // (Re)creates the general classes' side streams at the tuning's priority.
 cudaError_t make_side_streams(fwi_ctx* x)
