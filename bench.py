@@ -601,7 +601,8 @@ def run_ours(args):
             J_s, g_s = se.gradient()
         line["vs_strips"] = {"grad_rel_diff": float(np.linalg.norm(g_c - g_s) / np.linalg.norm(g_s)),
                              "misfit_equal": bool(J_c == J_s),
-                             "note": "the strip ring's gradient is within 5e-6 of the FP64 oracle on the 560 x 1700 workload"}
+                             "note": "the strip ring's gradient is within 5e-6 of the FP64 oracle on the "
+                                     "560 x 1700 workload"}
 
     # CPU baseline (the reference's own kernels, or their restatement) and the accuracy check
     if "cpu" not in skip and rank == 0 and world == 1:

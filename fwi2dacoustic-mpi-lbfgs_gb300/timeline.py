@@ -57,7 +57,8 @@ def report(path):
             st, en = a[base + c, v, 0] - t0, a[base + c, v, 1] - t0
             end = max(end, en.max())
             print(f"  {NAMES[c]:10s} items {len(v):6d}  first start {st.min() / 1e3:7.1f} us  last start "
-                  f"{st.max() / 1e3:7.1f}  last end {en.max() / 1e3:7.1f}  median item {np.median(en - st) / 1e3:6.2f} us")
+                  f"{st.max() / 1e3:7.1f}  last end {en.max() / 1e3:7.1f}  "
+                  f"median item {np.median(en - st) / 1e3:6.2f} us")
         bins = np.arange(0, end + 20000, 20000)
         print("  items active per 20 us bin (" + " / ".join(NAMES) + "):")
         for b0, b1 in zip(bins[:-1], bins[1:]):

@@ -4,8 +4,9 @@ with AddressSanitizer and UBSan preloaded and FWI_LIB pointing at
 libfwiemu.so.  Arguments: free surface, nt, nx, nz [, nseg [, fd_order [,
 x shift, z shift of the tile grid (fwi_tuning)]]].
 Prints one JSON line {J, J64, grad_rel, syn_rel, obs_call_same} (the last:
-fwi_gradient_obs returns fwi_gradient's result bit for bit).  With nseg > 0 the same gradient is also taken with checkpoints
-(FWI_STORE_SNAPSHOTS, nseg segments) in FP32 and FP16 storage (BF16 shares
+fwi_gradient_obs returns fwi_gradient's result bit for bit).  With nseg > 0
+the same gradient is also taken with checkpoints (FWI_STORE_SNAPSHOTS, nseg
+segments) in FP32 and FP16 storage (BF16 shares
 the FP16 path but for its rounding) and the line adds {snap_f32_rel,
 snap_f16_rel} (against FP64) and snap_f32_vs_strips."""
 import json

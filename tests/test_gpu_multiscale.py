@@ -48,7 +48,8 @@ def smooth(v, r):
             c = np.cumsum(p, axis=ax, dtype=np.float64)
             c = np.concatenate([np.zeros_like(np.take(c, [0], axis=ax)), c], axis=ax)
             n = out.shape[ax]
-            out = (np.take(c, np.arange(2 * r + 1, 2 * r + 1 + n), axis=ax) - np.take(c, np.arange(n), axis=ax)) / (2 * r + 1)
+            hi = np.take(c, np.arange(2 * r + 1, 2 * r + 1 + n), axis=ax)
+            out = (hi - np.take(c, np.arange(n), axis=ax)) / (2 * r + 1)
     return out.astype(np.float32)
 
 
