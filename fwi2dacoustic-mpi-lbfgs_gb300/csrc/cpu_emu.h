@@ -277,10 +277,31 @@ inline cudaError_t cudaGraphDestroy(cudaGraph_t) { return cudaSuccess; }
 inline cudaError_t cudaGraphExecDestroy(cudaGraphExec_t) { return cudaSuccess; }
 
 #define FWI_LAUNCH(kernel, grid, block, smem, stream, ...) fwi_emu::launch(kernel, grid, block, smem, __VA_ARGS__)
+#define FWI_LAUNCH_PDL(kernel, grid, block, smem, stream, ...) fwi_emu::launch(kernel, grid, block, smem, __VA_ARGS__)
 
 #else  // the real CUDA build
 
 #define FWI_DYN_SMEM(name) extern __shared__ __align__(16) unsigned char name[]
 #define FWI_LAUNCH(kernel, grid, block, smem, stream, ...) kernel<<<grid, block, smem, stream>>>(__VA_ARGS__)
+// A launch that may start while the previous kernel on its stream finishes
+// (programmatic dependent launch); the kernel waits for that kernel's results
+// with griddepcontrol.wait before it reads them (pdl_begin).
+template <typename... KArgs, typename... Args>
+inline cudaError_t fwi_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                                  Args... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+#define FWI_LAUNCH_PDL(kernel, grid, block, smem, stream, ...) fwi_launch_pdl(kernel, grid, block, smem, stream, __VA_ARGS__)
 
 #endif

@@ -416,9 +416,9 @@ long long launch_fwd_step8(fwi_ctx* x, StepParams& P, int n)
     const dim3 block(32, 8);
     const dim3 gpos((x->g.pnx + 1 + 31) / 32, (x->g.pnz + 1 + 7) / 8, n), gcell((x->g.pnx + 31) / 32, (x->g.pnz + 7) / 8, n);
     const Step8 B = step8_buffers(x);
-    FWI_LAUNCH(k8_uv, gpos, block, 0, x->st, P, B);
+    FWI_LAUNCH_PDL(k8_uv, gpos, block, 0, x->st, P, B);
     DIAG_SYNC("k8_uv");
-    FWI_LAUNCH(k8_fwd, gcell, block, 0, x->st, P, B);
+    FWI_LAUNCH_PDL(k8_fwd, gcell, block, 0, x->st, P, B);
     DIAG_SYNC("k8_fwd");
     return 2;
 }
@@ -429,18 +429,18 @@ long long launch_bwd_step8(fwi_ctx* x, StepParams& P, int n)
     const dim3 gpos((x->g.pnx + 1 + 31) / 32, (x->g.pnz + 1 + 7) / 8, n), gcell((x->g.pnx + 31) / 32, (x->g.pnz + 7) / 8, n);
     const Step8 B = step8_buffers(x);
     long long l = 3;
-    FWI_LAUNCH(k8_adj_uv, gpos, block, 0, x->st, P, B);
+    FWI_LAUNCH_PDL(k8_adj_uv, gpos, block, 0, x->st, P, B);
     DIAG_SYNC("k8_adj_uv");
-    FWI_LAUNCH(k8_adj, gcell, block, 0, x->st, P, B);
+    FWI_LAUNCH_PDL(k8_adj, gcell, block, 0, x->st, P, B);
     DIAG_SYNC("k8_adj");
     const int c0 = x->cell8_off[P.shot_base], nc = x->cell8_off[P.shot_base + n] - c0;
     if ((P.step - 1) % x->cfg.jump == 0 && nc > 0) {
-        FWI_LAUNCH(k8_inject, (nc + 127) / 128, 128, 0, x->st, P, x->cells8_d + c0, x->rec8_d, nc,
+        FWI_LAUNCH_PDL(k8_inject, (nc + 127) / 128, 128, 0, x->st, P, x->cells8_d + c0, x->rec8_d, nc,
                    (P.step - 1) / x->cfg.jump);
         DIAG_SYNC("k8_inject");
         ++l;
     }
-    FWI_LAUNCH(k8_rebuild, dim3((x->g.nx + 31) / 32, (x->g.nz + 7) / 8, n), block, 0, x->st, P, B);
+    FWI_LAUNCH_PDL(k8_rebuild, dim3((x->g.nx + 31) / 32, (x->g.nz + 7) / 8, n), block, 0, x->st, P, B);
     DIAG_SYNC("k8_rebuild");
     return l;
 }

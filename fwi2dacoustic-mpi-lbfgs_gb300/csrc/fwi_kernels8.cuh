@@ -185,10 +185,26 @@ __device__ __forceinline__ float psi_adj(const PsiSite& t, const float* psr, flo
     const float* a0z = a0x + 4 * n2;    const float* b0z = a0x + 5 * n2;                                   \
     const float* a1z = a0x + 6 * n2;    const float* b1z = a0x + 7 * n2;
 
+// The 8th-order passes run back to back on one stream, and on the small grids
+// they serve each pass is short, so the gap between launches is a large part of
+// a step.  They are launched as programmatic dependent launches: a pass may be
+// scheduled while the previous one finishes, waits here for that pass to
+// complete (its writes then visible) before it touches global memory, and at
+// once lets the next pass be scheduled in turn.  Without a programmatic
+// prerequisite (the first pass of a phase) the wait returns at once.
+__device__ __forceinline__ void pdl_begin()
+{
+#ifndef FWI_CPU_EMU
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
 // Forward, pass 1: u at positions (row, j), j = 0..pnx, and v at (kv, c),
 // kv = 0..pnz, of p^it, each with its CPML psi.
 __global__ void __launch_bounds__(256) k8_uv(const StepParams P, Step8 B)
 {
+    pdl_begin();
     const Geo& g = P.g;
     const Coef& cf = P.c;
     const int j = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
@@ -216,6 +232,7 @@ __global__ void __launch_bounds__(256) k8_uv(const StepParams P, Step8 B)
 // strips of p^{it+1}.
 __global__ void __launch_bounds__(256) k8_fwd(const StepParams P, Step8 B)
 {
+    pdl_begin();
     const Geo& g = P.g;
     const Coef& cf = P.c;
     const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
@@ -245,6 +262,7 @@ __global__ void __launch_bounds__(256) k8_fwd(const StepParams P, Step8 B)
 // It also forms the rebuild's interior u / v of p^{m-1} on the physical grid.
 __global__ void __launch_bounds__(256) k8_adj_uv(const StepParams P, Step8 B)
 {
+    pdl_begin();
     const Geo& g = P.g;
     const Coef& cf = P.c;
     const int j = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
@@ -318,6 +336,7 @@ __global__ void __launch_bounds__(256) k8_adj_uv(const StepParams P, Step8 B)
 // b^m = 2 b^{m+1} - b^{m+2} + K pbar in place over b^{m+2}.
 __global__ void __launch_bounds__(256) k8_adj(const StepParams P, Step8 B)
 {
+    pdl_begin();
     const Geo& g = P.g;
     const Coef& cf = P.c;
     const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
@@ -359,6 +378,7 @@ __global__ void __launch_bounds__(256) k8_adj(const StepParams P, Step8 B)
 __global__ void k8_inject(const StepParams P, const RecCell8* __restrict__ cells, const long long* __restrict__ syn_base,
                           int ncell, int k)
 {
+    pdl_begin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ncell) return;
     const RecCell8 rc = cells[i];
@@ -375,6 +395,7 @@ __global__ void k8_inject(const StepParams P, const RecCell8* __restrict__ cells
 // ((p^m - 2 p^{m-1} + p^{m-2}) / K on the strips).
 __global__ void __launch_bounds__(256) k8_rebuild(const StepParams P, Step8 B)
 {
+    pdl_begin();
     const Geo& g = P.g;
     const Coef& cf = P.c;
     const int ix = blockIdx.x * blockDim.x + threadIdx.x, iz = blockIdx.y * blockDim.y + threadIdx.y;
