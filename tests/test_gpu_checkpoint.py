@@ -13,7 +13,13 @@ checkpoint per time segment plus a recompute of the segment), so:
   * batched, plain per-shot and graph-replayed checkpointed gradients are
     bit-identical;
   * FWI_STORE_AUTO keeps the strip ring when the budget allows and falls
-    back to checkpoints (or FWI_ERR_NOMEM) when it does not.
+    back to checkpoints (or FWI_ERR_NOMEM) when it does not;
+  * on the full grids of the two checkpointing workloads (2000 x 6000, dx 5 m,
+    dt 0.5 ms and 800 x 2400, dx 10 m, dt 1 ms; 2 shots, 801 / 1001 steps in
+    round(sqrt(nt)) segments), where the FP64 oracle would take minutes, the
+    storages are compared with each other: identical traces and misfit, and
+    the checkpointed gradients within FULL_TOL of the strip ring's (measured
+    2.4e-6 / 4.6e-4 / 3.1e-3 on the larger grid, FP32 / FP16 / BF16).
 """
 import numpy as np
 import pytest
@@ -24,6 +30,7 @@ pytestmark = pytest.mark.gpu
 
 GRAD_TOL = 1e-4
 SNAP_TOL = {"f32": 1e-4, "f16": 1e-3, "bf16": 6e-3}
+FULL_TOL = {"f32": 1e-5, "f16": 2e-3, "bf16": 1.5e-2}
 
 
 def _engine(case, **kw):
@@ -110,3 +117,34 @@ def test_auto_storage_follows_the_budget(engine_lib, oracles):
     with pytest.raises(fwigpu.FwiError) as ei:
         _engine(case, store=fwigpu.STORE_AUTO, hbm_budget_mb=1)
     assert ei.value.status == -3                              # FWI_ERR_NOMEM
+
+
+@pytest.mark.parametrize("name,nt", [("c4", 801), ("c5", 1001)])
+def test_checkpoints_against_strips_on_full_grids(engine_lib, name, nt):
+    import fwigpu
+    import workloads
+    cfgkw, vtrue, vstart, shots = workloads.build(name, nshots=2, nt=nt)
+    assert (cfgkw["nz"], cfgkw["nx"]) == {"c4": (2000, 6000), "c5": (800, 2400)}[name]
+    v0 = (0.95 * vstart).astype(np.float32)            # residuals of the order of the data
+    nseg = int(round(np.sqrt(nt)))
+    with fwigpu.Engine(fwigpu.make_config(**cfgkw, store=fwigpu.STORE_STRIPS)) as e:
+        e.set_shots(shots)
+        e.set_model(vtrue)
+        obs = e.forward().copy()
+        e.set_model(v0)
+        e.set_observed(obs)
+        J, g = e.gradient()
+        syn = e.forward().copy()
+        assert e.stats()["store"] == fwigpu.STORE_STRIPS
+    for prec in ("f32", "f16", "bf16"):
+        cfg = fwigpu.make_config(**cfgkw, store=fwigpu.STORE_SNAPSHOTS, snapshots=nseg, snap_precision=prec)
+        with fwigpu.Engine(cfg) as e:
+            e.set_shots(shots)
+            e.set_model(v0)
+            e.set_observed(obs)
+            Js, gs = e.gradient()
+            st = e.stats()
+            assert np.array_equal(e.forward(), syn)
+        assert st["store"] == fwigpu.STORE_SNAPSHOTS and st["segments"] == nseg, st
+        assert Js == J, (prec, Js, J)
+        assert rel(gs, g) <= FULL_TOL[prec], (prec, rel(gs, g))
