@@ -532,7 +532,7 @@ long long launch_bwd_step(fwi_ctx* x, StepParams& P, int lo, int hi)
         P.gen_shots = n;
         const dim3 grid = gen_grid(x, cls, cnt, n);
         cudaStream_t cs = class_stream(x, cls);
-        if (x->tune.bwd_gen_blocks == 3) launch_bwd_edge<3>(cls, grid, block, cs, P);
+        if ((cls == 1 ? x->tune.bwd_zgen_blocks : x->tune.bwd_gen_blocks) == 3) launch_bwd_edge<3>(cls, grid, block, cs, P);
         else launch_bwd_edge<4>(cls, grid, block, cs, P);
         DIAG_SYNC("k_bwd_edge");
         ++l;
@@ -996,6 +996,7 @@ fwi_tuning default_tuning(const fwi_ctx* x)
     t.z_first = x->cfg.free_surface ? 8 : (int)round_up(std::max(8, np + 5), R);
     t.fwd_gen_blocks = 4;
     t.bwd_gen_blocks = 3;           // 80 registers: the psi-site tables made the 64-register variant 11% slower
+    t.bwd_zgen_blocks = 4;          // the z-general class alone: 1% faster per backward step at 4 (C2 grid)
     t.fwd_int_blocks = 6;
     t.bwd_int_blocks = 4;
     t.class_order = 1;
@@ -1810,7 +1811,7 @@ int fwi_set_stream(fwi_ctx* x, void* stream)
 int fwi_set_tuning(fwi_ctx* x, const fwi_tuning* t)
 {
     if (!x || !t) return FWI_ERR_ARG;
-    for (int i = 0; i < 6; ++i)
+    for (int i = 0; i < 5; ++i)
         if (t->reserved[i]) return fail(x, FWI_ERR_ARG, "fwi_tuning.reserved must be zero");
     const fwi_tuning d = default_tuning(x);
     fwi_tuning n = x->tune;
@@ -1825,6 +1826,7 @@ int fwi_set_tuning(fwi_ctx* x, const fwi_tuning* t)
     n.serial = pick(t->serial, d.serial);
     n.priority = pick(t->priority, d.priority);
     n.gen_grid = pick(t->gen_grid, d.gen_grid);
+    n.bwd_zgen_blocks = pick(t->bwd_zgen_blocks, d.bwd_zgen_blocks);
     const Geo& g = x->g;
     if (n.x_first < d.x_first || n.x_first % 4 || n.x_first >= g.pnx - g.npml - 4)
         return fail(x, FWI_ERR_ARG, "x_first must be a multiple of 4 from " + std::to_string(d.x_first));
@@ -1833,7 +1835,8 @@ int fwi_set_tuning(fwi_ctx* x, const fwi_tuning* t)
     if ((n.fwd_gen_blocks != 3 && n.fwd_gen_blocks != 4) || (n.bwd_gen_blocks != 3 && n.bwd_gen_blocks != 4) ||
         (n.fwd_int_blocks != 4 && n.fwd_int_blocks != 6) || (n.bwd_int_blocks != 3 && n.bwd_int_blocks != 4) ||
         (n.class_order != 1 && n.class_order != 2) || (n.serial != 1 && n.serial != 2) ||
-        (n.priority != 1 && n.priority != 2) || n.gen_grid < 1 || n.gen_grid > 5)
+        (n.priority != 1 && n.priority != 2) || n.gen_grid < 1 || n.gen_grid > 5 ||
+        (n.bwd_zgen_blocks != 3 && n.bwd_zgen_blocks != 4))
         return fail(x, FWI_ERR_ARG, "a fwi_tuning value outside its list");
     CK(cudaSetDevice(x->cfg.device));
     CK(cudaStreamSynchronize(x->st));

@@ -119,9 +119,10 @@ class FwiTuning(C.Structure):
     """fwi_tuning (include/fwi_gb300.h): run-time launch choices, 0 = default."""
     _fields_ = [("x_first", C.c_int), ("z_first", C.c_int), ("fwd_gen_blocks", C.c_int), ("bwd_gen_blocks", C.c_int),
                 ("fwd_int_blocks", C.c_int), ("bwd_int_blocks", C.c_int), ("class_order", C.c_int),
-                ("serial", C.c_int), ("priority", C.c_int), ("gen_grid", C.c_int), ("reserved", C.c_int * 6)]
+                ("serial", C.c_int), ("priority", C.c_int), ("gen_grid", C.c_int),
+                ("bwd_zgen_blocks", C.c_int), ("reserved", C.c_int * 5)]
     KEYS = ("x_first", "z_first", "fwd_gen_blocks", "bwd_gen_blocks", "fwd_int_blocks", "bwd_int_blocks",
-            "class_order", "serial", "priority", "gen_grid")
+            "class_order", "serial", "priority", "gen_grid", "bwd_zgen_blocks")
 
 
 class FwiLbfgsParam(C.Structure):

@@ -10,7 +10,8 @@ chosen at run time (include/fwi_gb300.h, ``fwi_tuning``):
   strip) classes and how wide the partial tiles at the far ends are;
 * the occupancy each heavy kernel's register budget is compiled for
   (``fwd_gen_blocks``, ``bwd_gen_blocks``, ``fwd_int_blocks``,
-  ``bwd_int_blocks``);
+  ``bwd_int_blocks``, and ``bwd_zgen_blocks`` for the z-general backward
+  class, whose best setting differs from that of the other general classes);
 * the launch order of the general classes, whether they run concurrently
   with the interior tiles and at which stream priority (``class_order``,
   ``serial``, ``priority``).
@@ -38,7 +39,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_CACHE = os.path.join(PKG, "tuning_cache.json")
 
 KNOBS = (("fwd_gen_blocks", (4, 3)), ("bwd_gen_blocks", (4, 3)), ("fwd_int_blocks", (6, 4)),
-         ("bwd_int_blocks", (4, 3)), ("class_order", (1, 2)), ("serial", (2, 1)), ("priority", (1, 2)))
+         ("bwd_int_blocks", (4, 3)), ("class_order", (1, 2)), ("serial", (2, 1)), ("priority", (1, 2)),
+         ("bwd_zgen_blocks", (4, 3)))
 MARGIN = 0.005                      # relative gain a candidate needs to replace the current best
 
 

@@ -243,6 +243,9 @@ int fwi_get_stats(const fwi_ctx *ctx, fwi_stats *out);
  *       which must be set again.
  *   fwd_gen_blocks, bwd_gen_blocks: resident blocks per SM the general-tile
  *       kernels are compiled for, 3 or 4 (default 4 forward, 3 backward);
+ *       bwd_gen_blocks applies to the x-general and corner classes;
+ *   bwd_zgen_blocks: the same for the z-general backward class, 3 or 4
+ *       (default 4);
  *   fwd_int_blocks: the interior forward kernel, 4 or 6 (default 6);
  *   bwd_int_blocks: the interior backward kernel, 3 or 4 (default 4);
  *   class_order: 1 launches the z-general class first (default), 2 the
@@ -266,7 +269,8 @@ typedef struct fwi_tuning {
     int serial;
     int priority;
     int gen_grid;
-    int reserved[6];       /* zero */
+    int bwd_zgen_blocks;
+    int reserved[5];       /* zero */
 } fwi_tuning;
 /* FWI_ERR_ARG for a value outside the lists above. */
 int fwi_set_tuning(fwi_ctx *ctx, const fwi_tuning *tuning);

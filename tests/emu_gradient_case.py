@@ -33,7 +33,8 @@ def main(fs, nt, nx=150, nz=90, nseg=0, order=4, xshift=0, zshift=0):
     if xshift or zshift:                 # another tile grid (fwi_tuning x_first / z_first)
         t = e.tuning()
         e.set_tuning({"x_first": t["x_first"] + xshift, "z_first": t["z_first"] + zshift,
-                      "fwd_gen_blocks": 3, "bwd_int_blocks": 3, "class_order": 2, "serial": 1, "gen_grid": 3})
+                      "fwd_gen_blocks": 3, "bwd_int_blocks": 3, "class_order": 2, "serial": 1, "gen_grid": 3,
+                      "bwd_zgen_blocks": 3})
         e.set_shots(case.eshots)
     e.set_model(case.vel)
     syn = e.split(e.forward())

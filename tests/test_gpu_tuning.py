@@ -41,9 +41,11 @@ def test_kernel_variants_are_bit_identical(engine_lib, oracles):
     flat = np.concatenate([o.ravel() for o in case.oracle_obs(o64)])
     (J0, g0), t0 = _grad(case, flat)
     assert (t0["fwd_gen_blocks"], t0["bwd_gen_blocks"], t0["fwd_int_blocks"], t0["bwd_int_blocks"],
-            t0["class_order"], t0["serial"], t0["priority"], t0["gen_grid"]) == (4, 3, 6, 4, 1, 2, 1, 1)
+            t0["class_order"], t0["serial"], t0["priority"], t0["gen_grid"], t0["bwd_zgen_blocks"]) == \
+        (4, 3, 6, 4, 1, 2, 1, 1, 4)
     assert t0["x_first"] % 4 == 0
-    for tuning in ({"fwd_gen_blocks": 3, "bwd_gen_blocks": 4}, {"fwd_int_blocks": 4, "bwd_int_blocks": 3},
+    for tuning in ({"fwd_gen_blocks": 3, "bwd_gen_blocks": 4, "bwd_zgen_blocks": 3},
+                   {"fwd_int_blocks": 4, "bwd_int_blocks": 3},
                    {"class_order": 2}, {"serial": 1}, {"priority": 2}, {"gen_grid": 2}, {"gen_grid": 5}):
         (J, g), t = _grad(case, flat, tuning)
         assert all(t[k] == v for k, v in tuning.items())
@@ -77,7 +79,8 @@ def test_tuning_rejects_bad_values(engine_lib, oracles):
     with case.engine() as e:
         t0 = e.tuning()
         for bad in ({"fwd_gen_blocks": 5}, {"fwd_int_blocks": 5}, {"bwd_int_blocks": 2}, {"class_order": 3},
-                    {"serial": 3}, {"priority": 3}, {"gen_grid": 6}, {"gen_grid": -1}, {"x_first": t0["x_first"] - 4},
+                    {"serial": 3}, {"priority": 3}, {"gen_grid": 6}, {"gen_grid": -1}, {"bwd_zgen_blocks": 5},
+                    {"x_first": t0["x_first"] - 4},
                     {"x_first": t0["x_first"] + 2},
                     {"z_first": t0["z_first"] + 1}, {"x_first": 100000}):
             with pytest.raises(fwigpu.FwiError) as ei:
