@@ -86,3 +86,35 @@ def test_status_strings(engine_lib):
     for s in range(0, -9, -1):
         assert engine_lib.fwi_status_string(s)
     assert engine_lib.fwi_version() >= 1
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The ctypes mirrors in fwigpu.py have the header's field names, offsets
+    and sizes: a C program built against include/fwi_gb300.h prints them.  A
+    field renamed in one place fails to compile; one moved or resized fails
+    the comparison."""
+    import shutil
+    import subprocess
+    import fwigpu
+    cc = shutil.which(os.environ.get("CC", "gcc"))
+    if not cc:
+        pytest.skip("no C compiler")
+    structs = {"fwi_config": fwigpu.FwiConfig, "fwi_shot": fwigpu.FwiShot, "fwi_stats": fwigpu.FwiStats,
+               "fwi_misfit": fwigpu.FwiMisfit, "fwi_tuning": fwigpu.FwiTuning,
+               "fwi_lbfgs_param": fwigpu.FwiLbfgsParam}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "fwi_gb300.h"', "int main(void) {"]
+    want = []
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        want.append(f"{cname} sizeof {C.sizeof(py)}")
+        for name, _ in py._fields_:
+            lines.append(f'printf("{cname} {name} %zu\\n", offsetof({cname}, {name}));')
+            want.append(f"{cname} {name} {getattr(py, name).offset}")
+    lines += ["return 0;", "}"]
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    r = subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    assert [g for g in got if g] == want
