@@ -47,7 +47,8 @@ def emu_lib():
     return B.build_emu(), libs
 
 
-GRAD_CASES = [(1, 150, 90, 0, 0), (0, 130, 70, 0, 0), (1, 130, 70, 8, 4), (0, 150, 90, 32, 16)]
+GRAD_CASES = [(1, 150, 90, 0, 0), (0, 130, 70, 0, 0), (1, 130, 70, 8, 4), (0, 150, 90, 32, 16),
+              (1, 64, 44, 0, 0)]                     # the last: no interior tile
 CASES = dict({f"grad-{fs}-{nx}-{nz}-{xs}-{zs}": ["emu_gradient_case.py", fs, 41, nx, nz, 0, 4, xs, zs]
               for fs, nx, nz, xs, zs in GRAD_CASES},
              checkpoints=["emu_gradient_case.py", 1, 41, 130, 70, 5],

@@ -104,8 +104,10 @@ def test_forward_seismograms(lib, oracles, fs):
 
 
 # 150 x 90: full-width edge tiles; 130 x 70: a last tile column under half a
-# tile wide and a last tile row of a few rows (partial general tiles).
-@pytest.mark.parametrize("fs,nx,nz", [(1, 150, 90), (0, 150, 90), (1, 130, 70), (0, 130, 70)])
+# tile wide and a last tile row of a few rows (partial general tiles); 64 x 44:
+# no interior tile at all, every tile takes the general path.
+@pytest.mark.parametrize("fs,nx,nz", [(1, 150, 90), (0, 150, 90), (1, 130, 70), (0, 130, 70),
+                                      (1, 64, 44), (0, 64, 44)])
 def test_gradient_against_fp64_oracle(lib, oracles, fs, nx, nz):
     O, o32, o64 = oracles
     case = Case(O, fs, seed=3 + fs, nx=nx, nz=nz)
