@@ -175,6 +175,28 @@ def test_batched_equals_one_shot_at_a_time(lib, oracles):
     assert np.allclose(g, gs, rtol=1e-9, atol=1e-12 * np.abs(g).max())
 
 
+def test_minimal_record_beside_a_long_one(lib, oracles):
+    """A shot of 2 * jump + 1 steps (two trace samples) batched with one of
+    261 steps: the active-prefix launches drop it after its last step."""
+    O, _, o64 = oracles
+    base = Case(O, 1, seed=5)
+    short = base.shot_specs[0][:4] + (ricker(2 * base.ecfg.jump + 1, base.ecfg.dt, 15.0),)
+    case = Case(O, 1, seed=5, shots=[short, base.shot_specs[1]])
+    assert [len(s.wav) for s in case.oshots] == [5, 261]
+    obs = case.oracle_obs(o64)
+    e = case.engine()
+    e.set_model(case.vel)
+    e.set_observed(np.concatenate([o.ravel() for o in obs]))
+    J, g = e.gradient()
+    J64, g64 = 0.0, np.zeros_like(g)
+    for s, ob in zip(case.oshots, obs):
+        j, gg, _ = o64.gradient(case.oracle_cfg_for(len(s.wav)), case.vel, [s], [ob])
+        J64 += j
+        g64 += gg
+    assert abs(J - J64) <= 1e-5 * J64, (J, J64)
+    assert rel(g, g64) <= GRAD_TOL, rel(g, g64)
+
+
 def test_repeated_gradients_are_deterministic(lib, oracles):
     O, _, o64 = oracles
     case = Case(O, 0, seed=11, nt=201)
@@ -211,6 +233,9 @@ def test_error_paths(lib, oracles):
     with pytest.raises(fwigpu.FwiError) as ei:
         e.set_shots([longer])
     assert ei.value.status == -1                    # nt > nt_max
+    with pytest.raises(fwigpu.FwiError) as ei:
+        e.set_shots([])
+    assert ei.value.status == -1                    # no shots
     # the context stays usable after rejected calls
     e.set_shots(case.eshots)
     e.set_model(case.vel)
