@@ -14,6 +14,7 @@
 #endif
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstddef>
 #include <cstdlib>
@@ -33,6 +34,8 @@ static __device__ __align__(256) double g_noalloc_trace_sums[FWI_NOALLOC_MAX_TRA
 namespace {
 
 constexpr int kVersion = 1;
+// Shots of one batch: the stencil launches put the shot in blockIdx.z.
+constexpr int MAX_SHOTS = 65535;
 
 inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
 
@@ -1349,6 +1352,7 @@ int fwi_set_model(fwi_ctx* x, const float* vel)
 int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
 {
     if (!x || nshots < 1 || !shots) return fail(x, FWI_ERR_ARG, "need at least one shot");
+    if (nshots > MAX_SHOTS) return fail(x, FWI_ERR_ARG, "at most " + std::to_string(MAX_SHOTS) + " shots per batch");
     CK(cudaSetDevice(x->cfg.device));
     const Geo& g = x->g;
     const int jump = x->cfg.jump;
@@ -1373,6 +1377,7 @@ int fwi_set_shots(fwi_ctx* x, int nshots, const fwi_shot* shots)
             return fail(x, FWI_ERR_GEOMETRY, "shot " + std::to_string(s) + ": source outside the model");
         for (int i = 0; i < sh.nt; ++i)
             if (!std::isfinite(sh.wavelet[i])) return fail(x, FWI_ERR_NONFINITE, "non-finite wavelet sample");
+        if (wav_tot + sh.nt > INT_MAX) return fail(x, FWI_ERR_ARG, "more than 2^31 - 1 wavelet samples in the batch");
         ShotDev& d = sd[s];
         d.nt = sh.nt; d.nt0 = (sh.nt - 1) / jump + 1; d.nr = sh.nr;
         d.src_r = iz + g.z0p; d.src_c = ix + g.x0p;

@@ -161,7 +161,9 @@ void     fwi_destroy(fwi_ctx *ctx);
 int fwi_set_model(fwi_ctx *ctx, const float *vel);
 
 /* All shots of an iteration (one fwi_init per MPI rank in the reference,
- * MBotOpt.c:51).  Allocates the per-shot device state. */
+ * MBotOpt.c:51).  Allocates the per-shot device state.  FWI_ERR_ARG for
+ * nshots outside 1 .. 65535 (the launches put the shot in the grid's z
+ * dimension) or more than 2^31 - 1 wavelet samples in the batch. */
 int fwi_set_shots(fwi_ctx *ctx, int nshots, const fwi_shot *shots);
 
 /* Observed traces, all shots concatenated, shot s as [nr_s][nt0_s]

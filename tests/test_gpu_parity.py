@@ -236,6 +236,9 @@ def test_error_paths(lib, oracles):
     with pytest.raises(fwigpu.FwiError) as ei:
         e.set_shots([])
     assert ei.value.status == -1                    # no shots
+    with pytest.raises(fwigpu.FwiError) as ei:
+        e.set_shots([case.eshots[0]] * 65536)
+    assert ei.value.status == -1                    # more shots than the launch grid's z extent
     # the context stays usable after rejected calls
     e.set_shots(case.eshots)
     e.set_model(case.vel)
