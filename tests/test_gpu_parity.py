@@ -197,6 +197,27 @@ def test_minimal_record_beside_a_long_one(lib, oracles):
     assert rel(g, g64) <= GRAD_TOL, rel(g, g64)
 
 
+def test_shot_without_receivers_adds_nothing(lib, oracles):
+    """A shot with no receivers is accepted, has no traces and no residual, so
+    a batch that adds one returns the other shot's misfit and gradient bit for
+    bit."""
+    import fwigpu
+    O, _, o64 = oracles
+    case = Case(O, 1, seed=5)
+    obs = case.oracle_obs(o64)
+    spec = case.eshots[0]
+    silent = fwigpu.ShotSpec(spec.src_x + 200.0, spec.src_z, np.zeros((0, 2), np.float32), spec.wavelet)
+    out = []
+    with case.engine() as e:
+        for shots in ([spec], [spec, silent]):
+            e.set_shots(shots)
+            e.set_model(case.vel)
+            e.set_observed(obs[0].ravel())
+            out.append(e.gradient())
+    (J1, g1), (J2, g2) = out
+    assert J1 == J2 and np.array_equal(g1, g2)
+
+
 def test_repeated_gradients_are_deterministic(lib, oracles):
     O, _, o64 = oracles
     case = Case(O, 0, seed=11, nt=201)
